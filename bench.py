@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 raster pipeline (one JSON line on rank 0).
+
+Workload (default): the 100k-triangle soup scene - 1920x1080, 4x MSAA, textured fragment
+shader over a 1024x1024 noise texture, 10% of triangles across the near plane. One step is
+one full frame: vertex stage, clipping/setup, order-preserving binning, per-tile raster and
+resolve. Inputs (mesh, texture) are resident in HBM for `value`; `e2e` streams the mesh from
+pinned host memory through rast_mesh_update and reads the image back every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 0|1|2] [--impl ours|reference]
+
+--impl reference times the reference's CPU path: the reference crate is Rust and cannot be
+built here, so this is the C restatement of that path (oracle/), with all host threads.
+Multi-GPU: a frame does not shard (every tile needs every triangle), so N processes render
+independent replicas and `value` sums them.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
+           1: "triangle soup 100k tris 1920x1080 4xMSAA",
+           2: "heightfield 2M tris 3840x2160 4xMSAA"}
+LAUNCHES_PER_FRAME = 6  # vertex, bin count, column scan, tile scan, scatter, raster
+
+
+def make_scene(cfg):
+    from rusterizer_gb300 import scenes
+    return {0: scenes.config0, 1: scenes.config1, 2: scenes.config2}[cfg]()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(cfg):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(str(cfg))
+    except Exception:
+        return None
+
+
+REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap",
+           0x8: "hw_slowdown", 0x10: "sync_boost", 0x20: "sw_thermal_slowdown",
+           0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+           0x100: "display_clock_setting"}
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
+                 "clocks_event_reasons.active", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 3:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+                bits = int(parts[2], 16) if parts[2].startswith("0x") else int(parts[2])
+            except ValueError:
+                continue
+            for b, n in REASONS.items():
+                if bits & b and n != "gpu_idle":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(scene, seconds, nthreads):
+    """The oracle (restated reference CPU path) on a bounded number of full frames."""
+    import oracle
+    n, t0 = 0, time.perf_counter()
+    shaded = 0
+    while True:
+        _, _, _, st, _, _ = oracle.render_scene(scene, nthreads=nthreads)
+        shaded = st["shaded_samples"]
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt, shaded
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    scene = make_scene(args.config)
+    import oracle
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        oracle.render_scene(scene, nthreads=cores)
+    times = []
+    shaded = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, _, st, _, _ = oracle.render_scene(scene, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+        shaded = st["shaded_samples"]
+    fps = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": CONFIGS[args.config], "config_index": args.config},
+        "shaded_samples_per_s": shaded * fps,
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full frames, row bands over {cores} threads "
+                                   "(the reference crate is Rust; no toolchain here)"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from rusterizer_gb300 import _lib, renderer, scenes
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    scene = make_scene(args.config)
+    W, H = scene["width"], scene["height"]
+    L = _lib.load()
+    r = renderer.Renderer(W, H, scene.get("msaa", 4), tile=args.tile)
+    r.set_clear_depth(scene.get("clear_depth", np.finfo(np.float32).max))
+    for i, t in enumerate(scene["textures"]):
+        r.uniforms().bind_texture(i, renderer.Texture(t))
+    blk = r.uniforms().write_block()
+    blk.view, blk.projection = scene["view"], scene["proj"]
+
+    def queue():
+        for d in scene["draws"]:
+            blk.world = d["world"]
+            r.render(d, renderer.VS_MVP, d.get("fs", 0))
+
+    r.set_profiling(True)
+    # synchronous warm-up frames size every buffer and validate the status
+    for _ in range(max(args.warmup, 3)):
+        queue()
+        r.framebuffer()
+        assert r.last_status == 0, r.last_status
+    stats = r.stats()
+    out_dev = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    ext = torch.cuda.ExternalStream(r.stream())
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    step_ms, stage = [], []
+    barrier()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(ext):
+                flush.zero_()  # L2 flush, outside the timed events
+                ev[k][0].record(ext)
+            queue()
+            st = L.rast_framebuffer_async(r._ctx, ctypes.c_void_p(out_dev.data_ptr()))
+            assert st == 0, st
+            with torch.cuda.stream(ext):
+                ev[k][1].record(ext)
+            ext.synchronize()
+            step_ms.append(ev[k][0].elapsed_time(ev[k][1]))
+            stage.append(r.stage_times())
+        barrier()
+    wall = time.perf_counter() - wall0
+    total_ms = sum(step_ms)
+    if pg:
+        t = torch.tensor([total_ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1000.0)
+    stage_mean = [sum(s[i] for s in stage) / len(stage) for i in range(5)]
+    names = ["vertex", "bin_count", "scan", "bin_scatter", "raster"]
+    dom = int(np.argmax(stage_mean))
+    bytes_frame = scenes.scene_bytes(scene)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = bytes_frame / (stage_mean[4] / 1000.0) / 1e9  # raster = the frame's HBM traffic
+
+    # e2e: stream the mesh from pinned host memory, render, read the image back
+    d0 = scene["draws"][0]
+    npos = torch.from_numpy(np.ascontiguousarray(d0["pos"])).pin_memory()
+    nuv = torch.from_numpy(np.ascontiguousarray(d0["uv"])).pin_memory()
+    nidx = torch.from_numpy(np.ascontiguousarray(d0["idx"]).view(np.int32)).pin_memory()
+    host_out = torch.empty(W * H, dtype=torch.int32).pin_memory()
+    e2 = renderer.Renderer(W, H, scene.get("msaa", 4), tile=args.tile)
+    e2.set_clear_depth(scene.get("clear_depth", np.finfo(np.float32).max))
+    for i, t in enumerate(scene["textures"]):
+        e2.uniforms().bind_texture(i, renderer.Texture(t))
+    m = renderer.Mesh(d0["pos"], d0["uv"], d0["idx"])
+    mh = e2.upload(m)
+    b2 = e2.uniforms().write_block()
+    b2.view, b2.projection, b2.world = scene["view"], scene["proj"], d0["world"]
+    fp = ctypes.POINTER(ctypes.c_float)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+
+    def e2e_step():
+        s = L.rast_mesh_update(e2._ctx, mh, ctypes.cast(npos.data_ptr(), fp),
+                               ctypes.cast(nuv.data_ptr(), fp), None, ctypes.cast(nidx.data_ptr(), u32p))
+        assert s == 0, s
+        e2.render(m, renderer.VS_MVP, d0.get("fs", 0))
+        s = L.rast_framebuffer(e2._ctx, ctypes.c_void_p(host_out.data_ptr()))
+        assert s == 0, s
+
+    for _ in range(max(args.warmup, 3)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        t = torch.tensor([e2e_s], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps / e2e_s
+    ref_img = r.framebuffer()
+    assert (host_out.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
+    h2d = npos.numel() * 4 + nuv.numel() * 4 + nidx.numel() * 4
+    e2.close()
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and args.cpu_seconds > 0:
+            fps, n, dt, _ = cpu_baseline(scene, args.cpu_seconds, 1)
+            cpu = {"value": fps, "unit": "frames/s", "cores": 1, "kind": "port",
+                   "sample": f"{n} full frames of the same scene in {dt:.1f} s, single thread"}
+        line = {
+            "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": CONFIGS[args.config], "config_index": args.config,
+                       "width": W, "height": H, "msaa": scene.get("msaa", 4),
+                       "triangles": scenes.scene_triangles(scene),
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "shaded_samples_per_s": stats["shaded_samples"] * value,
+            "shaded_samples_per_frame": stats["shaded_samples"],
+            "fs_invocations_per_frame": stats["fs_invocations"],
+            "stages_ms": dict(zip(names, stage_mean)),
+            "wall_ms_per_step": 1000 * wall / args.steps,
+            "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": committed_traffic(args.config),
+                         "algorithmic_bytes_per_frame": bytes_frame,
+                         "dominant_stage": names[dom]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": W * H * 4},
+            "gpu_launches": LAUNCHES_PER_FRAME * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    r.close()
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

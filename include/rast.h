@@ -1,0 +1,131 @@
+/*
+ * rast.h - C ABI of the GB300 (sm_103a) raster pipeline.
+ *
+ * Drop-in boundary for the per-frame raster path of the Rust software rasterizer
+ * NiklasJonsson/rusterizer. Each entry point names the reference interface it replaces
+ * (paths are inside that crate). Plain pointers and sizes only; no exceptions cross the ABI,
+ * every call returns a rast_status. A context owns its device memory and CUDA stream; host
+ * arrays passed in are only read during the call. One context per host thread (the reference
+ * Renderer is `&mut self` everywhere and not Sync).
+ *
+ * Conventions shared with the reference:
+ *   - matrices are row-major float[16] (Matrix.array, src/math/matrix.rs:7-16);
+ *   - the vertex shader is P * V * W * v (upstream demo src/main.rs:147-152);
+ *   - output is width*height ARGB u32, row-major, y = 0 at the top (src/color.rs:15-20,
+ *     src/rasterizer/mod.rs:315-345);
+ *   - 4x rotated-grid MSAA (src/rasterizer/mod.rs:23, :109-114); msaa = 1 is an extension
+ *     with one sample at the pixel centre.
+ */
+#ifndef RAST_H
+#define RAST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rast_status {
+    RAST_OK = 0,
+    RAST_INVALID_ARG = 1,      /* bad handle, size, index >= nverts, slot order, ... */
+    RAST_OOM = 2,              /* device allocation failed */
+    RAST_ADMISSION_REFUSED = 3,/* server: request does not fit the HBM budget */
+    RAST_BIN_OVERFLOW = 4,     /* bin capacity exceeded even after regrowth */
+    RAST_TIMEOUT = 5,          /* a bounded wait expired */
+    RAST_TEXTURE_OOB = 6,      /* a texel read ran past the texture (the reference panics in
+                                  Texture::read_texel, src/texture.rs:51-56); image still
+                                  produced, with texel 0 read instead */
+    RAST_CLIP_OVERFLOW = 7,    /* a clipped polygon exceeded 32 vertices (never observed) */
+    RAST_CUDA_ERROR = 8,
+    RAST_NOT_READY = 9         /* server: result not finished yet */
+} rast_status;
+
+typedef struct rast_ctx rast_ctx;
+typedef uint32_t rast_mesh;
+
+enum { RAST_VS_MVP = 0 };
+/* fragment shaders of the upstream demo, selected by id (src/main.rs:67-77) */
+enum { RAST_FS_TEXTURE = 0, RAST_FS_COLOR = 1, RAST_FS_DEBUG = 2 };
+
+const char* rast_status_string(rast_status s);
+
+/* Renderer::new / Rasterizer::new (src/render.rs:48-69, src/rasterizer/mod.rs:273-281).
+ * width, height in [1, 16384]; msaa 4 (reference) or 1. */
+rast_ctx* rast_create(int width, int height, int msaa, rast_status* status);
+void rast_destroy(rast_ctx* ctx);
+
+/* Depth clear value; the reference uses f32::MAX (src/rasterizer/buffers.rs:6). */
+rast_status rast_set_clear_depth(rast_ctx* ctx, float depth);
+/* Screen tile edge in pixels (8, 16, 32 or 64); 0 selects automatically. */
+rast_status rast_set_tile_size(rast_ctx* ctx, int tile);
+
+/* Upload a mesh (Mesh{vertices, indices, attributes}, src/mesh.rs:5-12) so that it stays
+ * resident. pos: nverts*3 f32; uv: nverts*2 f32; rgba: nverts*4 f32 or NULL (colour
+ * (0,0,0,0)); idx: ntris*3 u32, each < nverts (primitive_assembly would panic otherwise,
+ * src/render.rs:75-96). */
+rast_status rast_mesh_upload(rast_ctx* ctx, const float* pos, const float* uv, const float* rgba,
+                             uint32_t nverts, const uint32_t* idx, uint32_t ntris,
+                             rast_mesh* out);
+rast_status rast_mesh_free(rast_ctx* ctx, rast_mesh mesh);
+/* Overwrite a resident mesh with new host data of the same vertex and triangle counts (the
+ * reference borrows the mesh afresh on every render call, src/render.rs:98-110); copies only,
+ * no allocation. rgba must be given iff the mesh was uploaded with colours. */
+rast_status rast_mesh_update(rast_ctx* ctx, rast_mesh mesh, const float* pos, const float* uv,
+                             const float* rgba, const uint32_t* idx);
+
+/* Uniforms::bind_texture (src/uniform.rs:29-33): slot must equal the number already bound.
+ * rgba8 is w*h*4 bytes, row-major, (0,0) top-left (Texture, src/texture.rs:6-13). */
+rast_status rast_texture_upload(rast_ctx* ctx, int slot, const uint8_t* rgba8, int w, int h);
+
+/* Uniforms::write_block().{world, view, projection} (src/uniform.rs:4-45). */
+rast_status rast_set_uniforms(rast_ctx* ctx, const float world[16], const float view[16],
+                              const float proj[16]);
+
+/* Renderer::render(mesh, vertex_shader, fragment_shader) (src/render.rs:98-114): queues the
+ * draw with the current uniforms; draws keep submission order. */
+rast_status rast_draw(rast_ctx* ctx, rast_mesh mesh, int vs_id, int fs_id);
+
+/* Rasterizer::framebuffer (src/rasterizer/mod.rs:478-522): renders every queued draw,
+ * resolves, clears, and writes width*height ARGB u32 to argb_out (host or device pointer;
+ * NULL keeps the result on the device only). */
+rast_status rast_framebuffer(rast_ctx* ctx, uint32_t* argb_out);
+
+/* Same frame, enqueued on the context stream without waiting: no overflow re-run and no
+ * status readback (capacities come from earlier rast_framebuffer calls). argb_out must be a
+ * device pointer or NULL. Used by throughput loops; no counterpart in the reference. */
+rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out_device);
+
+/* Per-frame statistics of the last framebuffer call: samples written (popcount of
+ * depth-passed masks), fragment-shader invocations, texel reads past the texture. */
+rast_status rast_stats(rast_ctx* ctx, uint64_t* shaded_samples, uint64_t* fs_invocations,
+                       uint64_t* texture_oob);
+
+/* The context's CUDA stream (cudaStream_t) for event timing by the caller. */
+void* rast_stream(rast_ctx* ctx);
+
+/* Stage timing with CUDA events on the context stream. When enabled, rast_stage_times
+ * fills up to n floats (ms) of the last frame: vertex, bin-count, scan, scatter, raster. */
+rast_status rast_set_profiling(rast_ctx* ctx, int enable);
+int rast_stage_times(rast_ctx* ctx, float* ms, int n);
+
+/* ---- parity / debug ------------------------------------------------------------------ */
+
+/* Capture the per-sample buffers (depth f32, colour ARGB) of the next frames before resolve;
+ * the reference's DepthBuffer / ColorBuffer (src/rasterizer/buffers.rs:82-157). */
+rast_status rast_debug_capture_samples(rast_ctx* ctx, int enable);
+/* [y][x][sample] arrays of width*height*msaa elements; either pointer may be NULL. */
+rast_status rast_read_samples(rast_ctx* ctx, float* depth, uint32_t* color);
+/* Fragment log of the next frames: per fragment with a non-empty coverage mask, 4 u32 words
+ * {triangle, sub-triangle, (y << 16) | x, (depth-passed mask << 8) | coverage mask}. */
+rast_status rast_debug_log_enable(rast_ctx* ctx, uint64_t capacity);
+rast_status rast_debug_log_read(rast_ctx* ctx, uint32_t* out, uint64_t capacity,
+                                uint64_t* count);
+/* Runs one pipeline device function on the GPU for known-answer tests (op codes in
+ * rusterizer_gb300/csrc/rast_api.cu). */
+rast_status rast_debug_kat(int op, const void* in, size_t in_bytes, void* out, size_t out_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,236 @@
+// rast_internal.h - host-side engine state shared by the plain, batched and serving paths.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/rast.h"
+#include "rast_types.h"
+
+namespace rast {
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Device buffer that only grows (one cudaMalloc per growth, never per frame).
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n) {
+        if (n <= cap && p) return true;
+        size_t c = n > cap + cap / 2 ? n : cap + cap / 2;
+        if (c == 0) c = 1;
+        T* q = nullptr;
+        if (cudaMalloc(&q, c * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (p) cudaFree(p);
+        p = q;
+        cap = c;
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    ~DevBuf() { release(); }
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+};
+
+// Pinned host buffer for asynchronous copies.
+template <typename T>
+struct HostBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n) {
+        if (n <= cap && p) return true;
+        size_t c = n > cap + cap / 2 ? n : cap + cap / 2;
+        if (c == 0) c = 1;
+        T* q = nullptr;
+        if (cudaMallocHost(&q, c * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (p) cudaFreeHost(p);
+        p = q;
+        cap = c;
+        return true;
+    }
+    size_t size() const { return cap; }
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+};
+
+// A resident mesh (Mesh{vertices, indices, attributes}, src/mesh.rs:5-12).
+struct MeshRec {
+    float* pos = nullptr;
+    float* uv = nullptr;
+    float* rgba = nullptr;
+    uint32_t* idx = nullptr;
+    uint32_t nverts = 0, ntris = 0;
+    bool live = false;
+    size_t bytes() const {
+        return (size_t)nverts * (12 + 8 + (rgba ? 16 : 0)) + (size_t)ntris * 12;
+    }
+    rast_status upload(const float* hpos, const float* huv, const float* hrgba, uint32_t nv,
+                       const uint32_t* hidx, uint32_t nt, cudaStream_t st) {
+        nverts = nv;
+        ntris = nt;
+        auto alloc = [](void** p, size_t b) { return cudaMalloc(p, b ? b : 4) == cudaSuccess; };
+        if (!alloc((void**)&pos, (size_t)nv * 12) || !alloc((void**)&uv, (size_t)nv * 8) ||
+            (hrgba && !alloc((void**)&rgba, (size_t)nv * 16)) || !alloc((void**)&idx, (size_t)nt * 12)) {
+            cudaGetLastError();
+            release();
+            return RAST_OOM;
+        }
+        bool ok = true;
+        if (nv) {
+            ok &= cudaMemcpyAsync(pos, hpos, (size_t)nv * 12, cudaMemcpyHostToDevice, st) == cudaSuccess;
+            ok &= cudaMemcpyAsync(uv, huv, (size_t)nv * 8, cudaMemcpyHostToDevice, st) == cudaSuccess;
+            if (hrgba)
+                ok &= cudaMemcpyAsync(rgba, hrgba, (size_t)nv * 16, cudaMemcpyHostToDevice, st) == cudaSuccess;
+        }
+        if (nt) ok &= cudaMemcpyAsync(idx, hidx, (size_t)nt * 12, cudaMemcpyHostToDevice, st) == cudaSuccess;
+        ok &= cudaStreamSynchronize(st) == cudaSuccess;
+        if (!ok) {
+            release();
+            return RAST_CUDA_ERROR;
+        }
+        live = true;
+        return RAST_OK;
+    }
+    void release() {
+        if (pos) cudaFree(pos);
+        if (uv) cudaFree(uv);
+        if (rgba) cudaFree(rgba);
+        if (idx) cudaFree(idx);
+        pos = uv = rgba = nullptr;
+        idx = nullptr;
+        live = false;
+    }
+};
+
+// A resident RGBA8 texture, one u32 per texel (byte 0 = red).
+struct TexRec {
+    uint32_t* data = nullptr;
+    int w = 0, h = 0;
+    rast_status upload(const uint8_t* rgba8, int tw, int th, cudaStream_t st) {
+        w = tw;
+        h = th;
+        const size_t b = (size_t)tw * (size_t)th * 4;
+        if (cudaMalloc(&data, b) != cudaSuccess) {
+            cudaGetLastError();
+            data = nullptr;
+            return RAST_OOM;
+        }
+        if (cudaMemcpyAsync(data, rgba8, b, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            release();
+            return RAST_CUDA_ERROR;
+        }
+        return RAST_OK;
+    }
+    void release() {
+        if (data) cudaFree(data);
+        data = nullptr;
+    }
+};
+
+struct DrawJob {
+    const MeshRec* mesh = nullptr;
+    uint32_t mesh_id = 0;
+    const TexRec* tex = nullptr;
+    int fs = 0;
+    float mvp[16];
+};
+
+struct FrameJob {
+    int width = 0, height = 0, msaa = 4, ts = 16;
+    float clear_depth = 3.40282347e+38f;
+    std::vector<DrawJob> draws;
+    uint32_t* out_dev = nullptr;
+    float* dbg_depth = nullptr;
+    uint32_t* dbg_color = nullptr;
+    uint64_t bin_hint = 0;   // bins to reserve (0: default estimate)
+    uint32_t ntris_hint = 0;
+    uint64_t need = 0;       // bins the frame used (filled after a synchronous run)
+};
+
+// Device state block reset at the start of every launch sequence.
+struct DeviceState {
+    uint32_t status;
+    uint32_t pad;
+    unsigned long long stats[STAT_COUNT];
+    unsigned long long clip_used;
+    unsigned long long log_n;
+};
+
+struct Engine {
+    cudaStream_t stream = nullptr;
+    DevBuf<float4> vclip, vscr;
+    DevBuf<uint16_t> vcode;
+    DevBuf<unsigned long long> tri_rect;
+    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, bins;
+    DevBuf<float> clip_store;
+    DevBuf<unsigned long long> frame_need;
+    DevBuf<uint32_t> log;
+    bool log_on = false;
+    DevBuf<unsigned char> d_desc;
+    HostBuf<unsigned char> h_desc;
+    HostBuf<unsigned long long> h_need;
+    DeviceState* d_state = nullptr;
+    DeviceState* h_state = nullptr;
+    uint64_t clip_hint = 0;
+    bool sync_after = true;
+    bool profiling = false;
+    cudaEvent_t ev[6] = {};
+    float stage_ms[5] = {0, 0, 0, 0, 0};
+    uint32_t last_status = 0;
+    unsigned long long last_stats[STAT_COUNT] = {0, 0, 0, 0};
+    std::vector<FrameDev> h_frames;
+    std::vector<DrawDev> h_draws;
+    std::vector<ChunkDev> h_chunks;
+    std::vector<uint2> h_vblocks;
+    std::vector<unsigned char> h_scratch;
+    cudaEvent_t desc_done = nullptr;  // last descriptor upload finished reading h_desc
+    bool desc_pending = false, desc_valid = false;
+    size_t desc_bytes = 0;
+    unsigned char* d_desc_ptr = nullptr;
+
+    bool init() {
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (cudaMalloc(&d_state, sizeof(DeviceState)) != cudaSuccess) return false;
+        if (cudaMallocHost(&h_state, sizeof(DeviceState)) != cudaSuccess) return false;
+        std::memset(h_state, 0, sizeof(DeviceState));
+        for (auto& e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&desc_done, cudaEventDisableTiming) != cudaSuccess) return false;
+        return h_need.reserve(64);
+    }
+    ~Engine() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (desc_done) cudaEventDestroy(desc_done);
+        if (d_state) cudaFree(d_state);
+        if (h_state) cudaFreeHost(h_state);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+void mat4_mul(const float* a, const float* b, float* out);
+int choose_tile(int w, int h, int msaa, int req);
+rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs);
+
+}  // namespace rast

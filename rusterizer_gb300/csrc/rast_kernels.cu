@@ -1,0 +1,1124 @@
+// rast_kernels.cu - sm_103a kernels of the raster pipeline.
+//
+//   k_vertex       per vertex: MVP * v, divide, viewport, clip predicates       (HBM-bound)
+//   k_bin_count    per chunk of triangles: classify/clip, tile rectangle, per-chunk tile
+//                  histogram in shared memory
+//   k_scan_cols    per tile: exclusive prefix of the histograms over chunks
+//   k_scan_tiles   per frame: exclusive prefix over tiles -> bin ranges, capacity check
+//   k_bin_scatter  per chunk: order-preserving scatter of triangle ids into tile bins
+//   k_raster<S,TS> per tile: replays the tile's triangles in submission order with all
+//                  colour/depth samples in shared memory; coverage, depth test,
+//                  perspective-correct interpolation, fragment shader, resolve, store
+//
+// No kernel waits on another CTA; every loop is bounded by sizes read from descriptors.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rast_device.cuh"
+#include "rast_kernels.h"
+
+namespace rast {
+
+// ===================================================================== Sutherland-Hodgman
+
+__device__ __noinline__ int clip_polygon(const ClipVert in[3], ClipVert* poly) {
+    ClipVert buf[kMaxPoly];
+    ClipVert* cur = poly;
+    ClipVert* nxt = buf;
+    int cn = 3;
+    for (int k = 0; k < 3; ++k) cur[k] = in[k];
+    for (int plane = 0; plane < 6; ++plane) {
+        int on = 0;
+        for (int i = 0; i < cn; ++i) {
+            int pi = (i + cn - 1) % cn;
+            float dp = distance_measure(plane, cur[pi].p);
+            float dc = distance_measure(plane, cur[i].p);
+            bool pin = dp >= 0.0f, cin = dc >= 0.0f;
+            int need = (pin && cin) ? 1 : (pin && !cin) ? 1 : (!pin && cin) ? 2 : 0;
+            if (on + need > kMaxPoly) return -1;
+            if (pin && cin) {
+                nxt[on++] = cur[i];
+            } else if (pin && !cin) {
+                clip_intersect(cur[pi], dp, cur[i], dc, nxt[on++]);
+            } else if (!pin && cin) {
+                clip_intersect(cur[pi], dp, cur[i], dc, nxt[on++]);
+                nxt[on++] = cur[i];
+            }
+        }
+        ClipVert* t = cur;
+        cur = nxt;
+        nxt = t;
+        cn = on;
+        if (cn == 0) break;
+    }
+    if (cn > 0 && cur != poly)
+        for (int k = 0; k < cn; ++k) poly[k] = cur[k];
+    return cn;
+}
+
+// ===================================================================== helpers
+
+__device__ __forceinline__ unsigned long long pack_rect(uint32_t x0, uint32_t y0, uint32_t x1,
+                                                        uint32_t y1) {
+    return (unsigned long long)x0 | ((unsigned long long)y0 << 16) |
+           ((unsigned long long)x1 << 32) | ((unsigned long long)y1 << 48);
+}
+__device__ __forceinline__ void unpack_rect(unsigned long long r, uint32_t& x0, uint32_t& y0,
+                                            uint32_t& x1, uint32_t& y1) {
+    x0 = (uint32_t)(r & 0xFFFFu);
+    y0 = (uint32_t)((r >> 16) & 0xFFFFu);
+    x1 = (uint32_t)((r >> 32) & 0xFFFFu);
+    y1 = (uint32_t)((r >> 48) & 0xFFFFu);
+}
+__device__ __forceinline__ uint32_t rect_tiles(unsigned long long r) {
+    if (r == kRectEmpty) return 0;
+    uint32_t x0, y0, x1, y1;
+    unpack_rect(r, x0, y0, x1, y1);
+    return (x1 - x0 + 1) * (y1 - y0 + 1);
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// Block-wide exclusive scan of one u32 per thread (blockDim.x <= 1024). `tmp` holds 33 words.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* tmp, uint32_t& total) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? tmp[lane] : 0u;
+        uint32_t s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= (uint32_t)o) s += y;
+        }
+        tmp[lane] = s - w;
+        if (lane == 31) tmp[32] = s;
+    }
+    __syncthreads();
+    uint32_t r = tmp[warp] + x - v;
+    total = tmp[32];
+    __syncthreads();
+    return r;
+}
+
+// ===================================================================== vertex stage
+
+__global__ void __launch_bounds__(256) k_vertex(const DrawDev* __restrict__ draws,
+                                                const FrameDev* __restrict__ frames,
+                                                const uint2* __restrict__ vblocks, Scratch s) {
+    __shared__ float m[16];
+    const uint2 vb = vblocks[blockIdx.x];
+    const DrawDev* d = &draws[vb.x];
+    if (threadIdx.x < 16) m[threadIdx.x] = d->mvp[threadIdx.x];
+    __syncthreads();
+    const uint32_t v = vb.y + threadIdx.x;
+    if (v >= d->nverts) return;
+    const FrameDev* f = &frames[d->frame];
+    const float x = __ldg(d->pos + 3ull * v), y = __ldg(d->pos + 3ull * v + 1),
+                z = __ldg(d->pos + 3ull * v + 2);
+    // vertex shader P*V*W*v (upstream src/main.rs:147-152) with MVP folded on the host in the
+    // same dot order; Mat4 * Vec4 is src/math/vector.rs:219-240
+    float4 c = make_float4(dot4(m + 0, x, y, z, 1.0f), dot4(m + 4, x, y, z, 1.0f),
+                           dot4(m + 8, x, y, z, 1.0f), dot4(m + 12, x, y, z, 1.0f));
+    const uint32_t o = d->vbase + v;
+    s.vclip[o] = c;
+    s.vscr[o] = to_screen(c, (float)f->width, (float)f->height);
+    s.vcode[o] = (uint16_t)clip_code(c);
+}
+
+// ===================================================================== triangle classify
+
+// try_clip + divide + viewport + bounding box for one triangle (src/rasterizer/mod.rs:425-441).
+// Returns its tile rectangle (kRectEmpty when nothing can be covered) and, for a clipped
+// triangle, the offset of its polygon in the clip store.
+__device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t tri,
+                                  const Scratch& s, unsigned long long& rect, uint32_t& aux) {
+    rect = kRectEmpty;
+    aux = kNone;
+    const uint32_t i0 = __ldg(d.idx + 3ull * tri), i1 = __ldg(d.idx + 3ull * tri + 1),
+                   i2 = __ldg(d.idx + 3ull * tri + 2);
+    const uint32_t v[3] = {d.vbase + i0, d.vbase + i1, d.vbase + i2};
+    const float4 c0 = s.vclip[v[0]], c1 = s.vclip[v[1]], c2 = s.vclip[v[2]];
+    const int cls = clip_classify(tri2x_area(c0.x, c0.y, c1.x, c1.y, c2.x, c2.y), s.vcode[v[0]],
+                                  s.vcode[v[1]], s.vcode[v[2]]);
+    if (cls == 0) return;
+    uint32_t bx0 = 0xFFFFFFFFu, bx1 = 0, by0 = 0xFFFFFFFFu, by1 = 0;
+    if (cls == 1) {
+        const float4 sv[3] = {s.vscr[v[0]], s.vscr[v[1]], s.vscr[v[2]]};
+        pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
+        if (bx0 >= bx1 || by0 >= by1) return;
+    } else {
+        ClipVert in[3];
+        const float4 cc[3] = {c0, c1, c2};
+        const uint32_t ii[3] = {i0, i1, i2};
+        for (int k = 0; k < 3; ++k) {
+            in[k].p[0] = cc[k].x;
+            in[k].p[1] = cc[k].y;
+            in[k].p[2] = cc[k].z;
+            in[k].p[3] = cc[k].w;
+            if (d.rgba) {
+                for (int q = 0; q < 4; ++q) in[k].a[q] = __ldg(d.rgba + 4ull * ii[k] + q);
+            } else {
+                for (int q = 0; q < 4; ++q) in[k].a[q] = 0.0f;
+            }
+            in[k].a[4] = __ldg(d.uv + 2ull * ii[k]);
+            in[k].a[5] = __ldg(d.uv + 2ull * ii[k] + 1);
+        }
+        ClipVert poly[kMaxPoly];
+        const int n = clip_polygon(in, poly);
+        if (n < 0) {
+            atomicOr(s.status, ST_CLIP_OVERFLOW);
+            return;
+        }
+        if (n < 3) return;
+        const unsigned long long need = 1ull + 10ull * (unsigned long long)n;
+        const unsigned long long off = atomicAdd(s.clip_used, need);
+        if (off + need > s.clip_cap) {
+            atomicOr(s.status, ST_CLIP_STORE_OVERFLOW);
+            return;
+        }
+        float* st = s.clip_store + off;
+        st[0] = __int_as_float(n);
+        float4 sc[kMaxPoly];
+        for (int k = 0; k < n; ++k) {
+            float4 cp = make_float4(poly[k].p[0], poly[k].p[1], poly[k].p[2], poly[k].p[3]);
+            sc[k] = to_screen(cp, (float)f.width, (float)f.height);
+            float* o = st + 1 + 10 * k;
+            o[0] = sc[k].x;
+            o[1] = sc[k].y;
+            o[2] = sc[k].z;
+            o[3] = sc[k].w;
+            for (int q = 0; q < 6; ++q) o[4 + q] = poly[k].a[q];
+        }
+        // fan [v0, v(i+1), v(i+2)] (src/rasterizer/clipping.rs:185-190): union of the pixel boxes
+        for (int t = 0; t + 2 < n; ++t) {
+            const float4 tv[3] = {sc[0], sc[t + 1], sc[t + 2]};
+            uint32_t a0, a1, b0, b1;
+            pixel_bbox(tv, f.width, f.height, a0, a1, b0, b1);
+            if (a0 >= a1 || b0 >= b1) continue;
+            bx0 = min(bx0, a0);
+            bx1 = max(bx1, a1);
+            by0 = min(by0, b0);
+            by1 = max(by1, b1);
+        }
+        aux = (uint32_t)off;
+        if (bx0 >= bx1 || by0 >= by1) return;
+    }
+    const uint32_t ts = (uint32_t)f.ts;
+    rect = pack_rect(bx0 / ts, by0 / ts, (bx1 - 1) / ts, (by1 - 1) / ts);
+}
+
+// ===================================================================== binning: count
+
+__global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ chunks,
+                                                   const DrawDev* __restrict__ draws,
+                                                   const FrameDev* __restrict__ frames,
+                                                   Scratch s) {
+    extern __shared__ uint32_t hist[];
+    const ChunkDev ch = chunks[blockIdx.x];
+    const DrawDev& d = draws[ch.draw];
+    const FrameDev& f = frames[d.frame];
+    const uint32_t nt = f.ntiles, tx = f.tiles_x;
+    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) hist[t] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < ch.tri_count; i += blockDim.x) {
+        const uint32_t tri = ch.tri_begin + i;
+        unsigned long long rect;
+        uint32_t aux;
+        classify_triangle(d, f, tri, s, rect, aux);
+        const uint32_t g = f.rect_base + d.tbase + tri;
+        s.tri_rect[g] = rect;
+        s.tri_aux[g] = aux;
+        if (rect != kRectEmpty) {
+            uint32_t x0, y0, x1, y1;
+            unpack_rect(rect, x0, y0, x1, y1);
+            for (uint32_t y = y0; y <= y1; ++y)
+                for (uint32_t x = x0; x <= x1; ++x) atomicAdd(&hist[y * tx + x], 1u);
+        }
+    }
+    __syncthreads();
+    uint32_t* row = s.counts + f.count_base + (unsigned long long)ch.row * nt;
+    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) row[t] = hist[t];
+}
+
+// ===================================================================== binning: scans
+
+// One block per 32-tile group of a frame; 32 segments of chunks per tile.
+__global__ void __launch_bounds__(1024) k_scan_cols(const FrameDev* __restrict__ frames,
+                                                    int nframes, Scratch s) {
+    __shared__ uint32_t part[32][33];
+    __shared__ int s_frame;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nframes;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (frames[mid].group_begin <= blockIdx.x) lo = mid; else hi = mid;
+        }
+        s_frame = lo;
+    }
+    __syncthreads();
+    const FrameDev& f = frames[s_frame];
+    const uint32_t tl = threadIdx.x & 31u, seg = threadIdx.x >> 5;
+    const uint32_t t = (blockIdx.x - f.group_begin) * 32u + tl;
+    const uint32_t R = f.nchunks, nt = f.ntiles;
+    const uint32_t r0 = (uint32_t)((unsigned long long)R * seg / 32u);
+    const uint32_t r1 = (uint32_t)((unsigned long long)R * (seg + 1) / 32u);
+    uint32_t* base = s.counts + f.count_base;
+    uint32_t sum = 0;
+    if (t < nt)
+        for (uint32_t r = r0; r < r1; ++r) sum += base[(unsigned long long)r * nt + t];
+    part[seg][tl] = sum;
+    __syncthreads();
+    if (seg == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < 32; ++k) {
+            uint32_t c = part[k][tl];
+            part[k][tl] = run;
+            run += c;
+        }
+        if (t < nt) s.tile_count[f.tile_begin + t] = run;
+    }
+    __syncthreads();
+    if (t < nt) {
+        uint32_t run = part[seg][tl];
+        for (uint32_t r = r0; r < r1; ++r) {
+            uint32_t* p = &base[(unsigned long long)r * nt + t];
+            uint32_t c = *p;
+            *p = run;
+            run += c;
+        }
+    }
+}
+
+// One block (1024 threads) per frame: tile_start = exclusive prefix of tile_count.
+__global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict__ frames,
+                                                     Scratch s) {
+    __shared__ uint32_t tmp[33];
+    const FrameDev& f = frames[blockIdx.x];
+    const uint32_t nt = f.ntiles;
+    const uint32_t per = (nt + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = threadIdx.x * per, b = min(nt, a + per);
+    uint32_t loc = 0;
+    for (uint32_t t = a; t < b; ++t) loc += s.tile_count[f.tile_begin + t];
+    uint32_t total;
+    uint32_t run = block_excl_scan(loc, tmp, total);
+    for (uint32_t t = a; t < b; ++t) {
+        uint32_t c = s.tile_count[f.tile_begin + t];
+        s.tile_start[f.tile_begin + t] = run;
+        run += c;
+    }
+    if (threadIdx.x == 0) {
+        s.frame_need[blockIdx.x] = total;
+        if ((unsigned long long)total > f.bin_cap) atomicOr(s.status, ST_BIN_OVERFLOW);
+    }
+}
+
+// ===================================================================== binning: scatter
+
+constexpr int kScatterThreads = 256;
+constexpr int kPairsPerBatch = 512;  // (triangle, tile) pairs ranked per batch
+constexpr int kHashSlots = 1024;     // open-addressing table over tile ids, load <= 0.5
+constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t hash_slot(uint32_t t) {
+    return (t * 2654435761u) >> (32 - 10);
+}
+
+// Ranks every (triangle, tile) pair of a chunk in submission order: per batch, a bit per
+// triangle per touched tile (hmask) gives each pair its rank among the batch's pairs of the
+// same tile; run_off carries each tile's running position across batches.
+__global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
+    const ChunkDev* __restrict__ chunks, const DrawDev* __restrict__ draws,
+    const FrameDev* __restrict__ frames, Scratch s) {
+    extern __shared__ uint32_t run_off[];
+    __shared__ uint32_t hkey[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots][kScatterThreads / 32];
+    __shared__ uint16_t slot_list[kPairsPerBatch];
+    __shared__ uint32_t nslots;
+    __shared__ uint32_t tmp[33];
+    __shared__ unsigned long long rect0;
+    if (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) return;
+    const ChunkDev ch = chunks[blockIdx.x];
+    const DrawDev& d = draws[ch.draw];
+    const FrameDev& f = frames[d.frame];
+    const uint32_t nt = f.ntiles, tx = f.tiles_x;
+    const uint32_t* crow = s.counts + f.count_base + (unsigned long long)ch.row * nt;
+    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x)
+        run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
+    for (uint32_t h = threadIdx.x; h < (uint32_t)kHashSlots; h += blockDim.x) {
+        hkey[h] = kHashEmpty;
+#pragma unroll
+        for (int w = 0; w < kScatterThreads / 32; ++w) hmask[h][w] = 0;
+    }
+    if (threadIdx.x == 0) nslots = 0;
+    __syncthreads();
+    uint32_t* bins = s.bins + f.bin_base;
+    const unsigned long long cap = f.bin_cap;
+    const uint32_t gbase = f.rect_base + d.tbase + ch.tri_begin;
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+    uint32_t base = 0;
+    while (base < ch.tri_count) {
+        const uint32_t i = base + threadIdx.x;
+        const bool live = i < ch.tri_count;
+        const unsigned long long rect = live ? s.tri_rect[gbase + i] : kRectEmpty;
+        const uint32_t n = rect_tiles(rect);
+        uint32_t total;
+        const uint32_t excl = block_excl_scan(n, tmp, total);
+        if (threadIdx.x == 0) {
+            tmp[0] = n;
+            rect0 = rect;
+        }
+        __syncthreads();
+        const uint32_t n0 = tmp[0];
+        const unsigned long long r0 = rect0;
+        __syncthreads();
+        const uint32_t frame_tri = d.tbase + ch.tri_begin + i;  // bin entry: triangle in frame
+        if (n0 > (uint32_t)kPairsPerBatch) {
+            // a single large triangle: its tiles are distinct, each takes the next position
+            const uint32_t g0 = d.tbase + ch.tri_begin + base;
+            uint32_t x0, y0, x1, y1;
+            unpack_rect(r0, x0, y0, x1, y1);
+            const uint32_t w = x1 - x0 + 1;
+            for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
+                const uint32_t t = (y0 + k / w) * tx + x0 + k % w;
+                const uint32_t pos = run_off[t];
+                if (pos < cap) bins[pos] = g0;
+                run_off[t] = pos + 1;
+            }
+            __syncthreads();
+            base += 1;
+            continue;
+        }
+        const bool part = live && (excl + n <= (uint32_t)kPairsPerBatch);
+        const uint32_t take = __syncthreads_count(part);
+        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+        if (part && n) unpack_rect(rect, x0, y0, x1, y1);
+        if (part && n) {
+            for (uint32_t y = y0; y <= y1; ++y)
+                for (uint32_t x = x0; x <= x1; ++x) {
+                    const uint32_t t = y * tx + x;
+                    uint32_t h = hash_slot(t);
+                    while (true) {
+                        const uint32_t old = atomicCAS(&hkey[h], kHashEmpty, t);
+                        if (old == kHashEmpty) {
+                            slot_list[atomicAdd(&nslots, 1u)] = (uint16_t)h;
+                            break;
+                        }
+                        if (old == t) break;
+                        h = (h + 1) & (kHashSlots - 1);
+                    }
+                    atomicOr(&hmask[h][warp], 1u << lane);
+                }
+        }
+        __syncthreads();
+        if (part && n) {
+            for (uint32_t y = y0; y <= y1; ++y)
+                for (uint32_t x = x0; x <= x1; ++x) {
+                    const uint32_t t = y * tx + x;
+                    uint32_t h = hash_slot(t);
+                    while (hkey[h] != t) h = (h + 1) & (kHashSlots - 1);
+                    uint32_t before = __popc(hmask[h][warp] & lanemask_lt());
+                    for (uint32_t w2 = 0; w2 < warp; ++w2) before += __popc(hmask[h][w2]);
+                    const uint32_t pos = run_off[t] + before;
+                    if (pos < cap) bins[pos] = frame_tri;
+                }
+        }
+        __syncthreads();
+        const uint32_t ns = nslots;
+        for (uint32_t j = threadIdx.x; j < ns; j += blockDim.x) {
+            const uint32_t h = slot_list[j];
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < kScatterThreads / 32; ++w2) {
+                cnt += __popc(hmask[h][w2]);
+                hmask[h][w2] = 0;
+            }
+            run_off[hkey[h]] += cnt;
+            hkey[h] = kHashEmpty;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) nslots = 0;
+        __syncthreads();
+        base += take;
+    }
+}
+
+// ===================================================================== raster
+
+constexpr int kRasterThreads = 256;
+
+template <int S, int TS>
+struct RasterCfg {
+    static constexpr int NPIX = TS * TS;
+    static constexpr int IC = 256;                 // items (triangles after clipping) per batch
+    static constexpr int FC = (TS >= 32) ? 512 : 768;  // fragments per flush
+};
+
+template <int S, int TS>
+struct RasterSmem {
+    using C = RasterCfg<S, TS>;
+    float zb[C::NPIX * S];
+    uint32_t cb[C::NPIX * S];
+    // items (struct of arrays)
+    float ipx[3][C::IC], ipy[3][C::IC], inx[3][C::IC], iny[3][C::IC];
+    float iz[3][C::IC], iw[3][C::IC], iinv[C::IC];
+    float iat[3][6][C::IC];
+    uint32_t irect[C::IC];
+    uint32_t itri[C::IC];
+    uint16_t isub[C::IC];
+    uint32_t idraw[C::IC];
+    uint32_t ipfx[C::IC + 1];
+    // fragments
+    float fz[S][C::FC];
+    uint16_t fitem[C::FC];
+    uint16_t fpix[C::FC];
+    uint16_t fslot[C::FC];
+    uint16_t plist[C::FC];
+    uint8_t fcov[C::FC];
+    uint8_t fdm[C::FC];
+    uint32_t pcnt[C::NPIX];
+    uint32_t poff[C::NPIX];
+    uint16_t lastw[C::NPIX * S];
+    float inv255[256];
+    uint32_t tmp[40];
+    uint32_t misc[8];
+};
+
+template <int S, int TS>
+size_t raster_smem_bytes() { return sizeof(RasterSmem<S, TS>); }
+
+__device__ __forceinline__ uint32_t find_draw(const DrawDev* __restrict__ draws,
+                                              const FrameDev& f, uint32_t g) {
+    uint32_t lo = f.draw_begin, hi = f.draw_begin + f.draw_count;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (draws[mid].tbase <= g) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Depth test in submission order for the staged fragments, then shading; see the per-step
+// comments. All threads of the block call this with the same nfrag.
+template <int S, int TS>
+__device__ void raster_flush(RasterSmem<S, TS>& sm, uint32_t nfrag, const DrawDev* __restrict__ draws,
+                             const Scratch& s, uint32_t X0, uint32_t Y0, unsigned long long& shaded,
+                             unsigned long long& fsinv, unsigned long long& oobc) {
+    using C = RasterCfg<S, TS>;
+    // 1. bucket fragments by pixel (arbitrary slot; restored to submission order in step 4)
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x)
+        sm.fslot[f] = (uint16_t)atomicAdd(&sm.pcnt[sm.fpix[f]], 1u);
+    __syncthreads();
+    // 2. pixel offsets: each thread scans a contiguous run of pixels
+    {
+        constexpr int PER = (C::NPIX + kRasterThreads - 1) / kRasterThreads;
+        const uint32_t a = threadIdx.x * PER;
+        uint32_t loc = 0;
+#pragma unroll
+        for (int k = 0; k < PER; ++k)
+            if (a + k < (uint32_t)C::NPIX) loc += sm.pcnt[a + k];
+        uint32_t total;
+        uint32_t run = block_excl_scan(loc, sm.tmp, total);
+#pragma unroll
+        for (int k = 0; k < PER; ++k)
+            if (a + k < (uint32_t)C::NPIX) {
+                sm.poff[a + k] = run;
+                run += sm.pcnt[a + k];
+            }
+    }
+    __syncthreads();
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x)
+        sm.plist[sm.poff[sm.fpix[f]] + sm.fslot[f]] = (uint16_t)f;
+    __syncthreads();
+    // 3+4. per pixel, in submission order: depth_coverage (strict <, src/rasterizer/mod.rs:
+    // 363-378) then the depth writes of write_pixel (mod.rs:380-397); remember the last writer
+    // of each sample so that only its colour lands
+    for (uint32_t p = threadIdx.x; p < (uint32_t)C::NPIX; p += blockDim.x) {
+        const uint32_t c = sm.pcnt[p];
+        if (!c) continue;
+        const uint32_t o = sm.poff[p];
+        for (uint32_t j = 1; j < c; ++j) {  // insertion sort: fragment index = submission order
+            const uint16_t v = sm.plist[o + j];
+            uint32_t k = j;
+            while (k > 0 && sm.plist[o + k - 1] > v) {
+                sm.plist[o + k] = sm.plist[o + k - 1];
+                --k;
+            }
+            sm.plist[o + k] = v;
+        }
+        float z[S];
+#pragma unroll
+        for (int q = 0; q < S; ++q) z[q] = sm.zb[p * S + q];
+        for (uint32_t j = 0; j < c; ++j) {
+            const uint32_t f = sm.plist[o + j];
+            const uint32_t cov = sm.fcov[f];
+            uint32_t dm = 0;
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+                if ((cov >> q) & 1u) {
+                    const float fzq = sm.fz[q][f];
+                    if (fzq < z[q]) {
+                        dm |= 1u << q;
+                        z[q] = fzq;
+                        sm.lastw[p * S + q] = (uint16_t)f;
+                    }
+                }
+            sm.fdm[f] = (uint8_t)dm;
+            if (s.log) {
+                const unsigned long long slot = atomicAdd(s.log_n, 1ull);
+                if (slot < s.log_cap) {
+                    const uint32_t it = sm.fitem[f];
+                    uint32_t* L = s.log + 4ull * slot;
+                    L[0] = sm.itri[it];
+                    L[1] = sm.isub[it];
+                    L[2] = ((Y0 + p / TS) << 16) | (X0 + p % TS);
+                    L[3] = (dm << 8) | cov;
+                } else {
+                    atomicOr(s.status, ST_LOG_OVERFLOW);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < S; ++q) sm.zb[p * S + q] = z[q];
+        sm.pcnt[p] = 0;
+    }
+    __syncthreads();
+    // 5. shading of every fragment that passed the depth test (Fragment::interpolate,
+    // mod.rs:69-100, then the fragment shader); colour lands where it is the last writer
+    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
+        const uint32_t dm = sm.fdm[f];
+        if (!dm) continue;
+        const uint32_t it = sm.fitem[f];
+        const uint32_t p = sm.fpix[f];
+        const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
+        float xs, ys;
+        interp_point<S>(x, y, dm, xs, ys);
+        const float e0 = edge_eval(sm.inx[0][it], sm.iny[0][it], sm.ipx[0][it], sm.ipy[0][it], xs, ys);
+        const float e1 = edge_eval(sm.inx[1][it], sm.iny[1][it], sm.ipx[1][it], sm.ipy[1][it], xs, ys);
+        const float e2 = edge_eval(sm.inx[2][it], sm.iny[2][it], sm.ipx[2][it], sm.ipy[2][it], xs, ys);
+        float u, v, w;
+        persp_bary(e0, e1, e2, sm.iw[0][it], sm.iw[1][it], sm.iw[2][it], u, v, w);
+        const DrawDev& d = draws[sm.idraw[it]];
+        float col[4];
+        if (d.fs == 0) {
+            // FS::Texture (upstream src/main.rs:214-216)
+            const float tu = sm.iat[0][4][it] * u + sm.iat[1][4][it] * v + sm.iat[2][4][it] * w;
+            const float tv = sm.iat[0][5][it] * u + sm.iat[1][5][it] * v + sm.iat[2][5][it] * w;
+            bool oob = false;
+            tex_sample(d.tex, d.tex_w, d.tex_h, tu, tv, sm.inv255, col, oob);
+            if (oob) ++oobc;
+        } else if (d.fs == 1) {
+            // FS::Color (upstream src/main.rs:217)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                col[q] = sm.iat[0][q][it] * u + sm.iat[1][q][it] * v + sm.iat[2][q][it] * w;
+        } else {
+            // FS::Debug (upstream src/main.rs:218-220): grayscale(frag_coords.depths[0])
+            const float g = sm.fz[0][f];
+            col[0] = g;
+            col[1] = g;
+            col[2] = g;
+            col[3] = 1.0f;
+        }
+        const uint32_t argb = to_argb(col[0], col[1], col[2], col[3]);
+#pragma unroll
+        for (int q = 0; q < S; ++q)
+            if (((dm >> q) & 1u) && sm.lastw[p * S + q] == f) sm.cb[p * S + q] = argb;
+        shaded += __popc(dm);
+        fsinv += 1;
+    }
+    __syncthreads();
+}
+
+template <int S, int TS>
+__global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __restrict__ frames,
+                                                           int nframes, uint32_t tile_offset,
+                                                           const DrawDev* __restrict__ draws,
+                                                           Scratch s) {
+    using C = RasterCfg<S, TS>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RasterSmem<S, TS>& sm = *reinterpret_cast<RasterSmem<S, TS>*>(smem_raw);
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nframes;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (frames[mid].tile_begin <= tile_offset + blockIdx.x) lo = mid; else hi = mid;
+        }
+        sm.misc[0] = (uint32_t)lo;
+    }
+    __syncthreads();
+    const FrameDev& f = frames[sm.misc[0]];
+    const uint32_t gt = tile_offset + blockIdx.x;
+    const uint32_t lt = gt - f.tile_begin;
+    const uint32_t X0 = (lt % f.tiles_x) * TS, Y0 = (lt / f.tiles_x) * TS;
+    const uint32_t W = f.width, H = f.height;
+    for (uint32_t i = threadIdx.x; i < (uint32_t)(C::NPIX * S); i += blockDim.x) {
+        sm.zb[i] = f.clear_depth;
+        sm.cb[i] = kClearColor;
+    }
+    for (uint32_t i = threadIdx.x; i < (uint32_t)C::NPIX; i += blockDim.x) sm.pcnt[i] = 0;
+    sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
+    __syncthreads();
+    unsigned long long shaded = 0, fsinv = 0, oobc = 0;
+    const bool overflow = (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) != 0;
+    const uint32_t nent = overflow ? 0u : s.tile_count[gt];
+    const uint32_t* bins = s.bins + f.bin_base + (overflow ? 0u : s.tile_start[gt]);
+
+    for (uint32_t e0 = 0; e0 < nent;) {
+        // ---- A. entries -> items (sub-triangles after clipping, in fan order)
+        const uint32_t e = e0 + threadIdx.x;
+        uint32_t g = 0, aux = kNone, nitems = 0;
+        if (e < nent) {
+            g = bins[e];
+            aux = s.tri_aux[f.rect_base + g];
+            nitems = (aux == kNone) ? 1u : (uint32_t)__float_as_int(s.clip_store[aux]) - 2u;
+        }
+        uint32_t itot;
+        const uint32_t iex = block_excl_scan(nitems, sm.tmp, itot);
+        const bool part = (e < nent) && (iex + nitems <= (uint32_t)C::IC);
+        const uint32_t take = __syncthreads_count(part);
+        if (part && threadIdx.x == take - 1) sm.misc[1] = iex + nitems;
+        if (part) {
+            const uint32_t di = find_draw(draws, f, g);
+            const DrawDev& d = draws[di];
+            float4 sv[3];
+            for (uint32_t k = 0; k < nitems; ++k) {
+                const uint32_t it = iex + k;
+                float at[3][6];
+                if (aux == kNone) {
+                    const uint32_t tri = g - d.tbase;
+                    const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
+                                            __ldg(d.idx + 3ull * tri + 2)};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        sv[q] = s.vscr[d.vbase + ii[q]];
+                        if (d.rgba) {
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
+                        }
+                        at[q][4] = __ldg(d.uv + 2ull * ii[q]);
+                        at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
+                    }
+                } else {
+                    const float* st = s.clip_store + aux + 1;
+                    const uint32_t vi[3] = {0u, k + 1, k + 2};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const float* o = st + 10 * vi[q];
+                        sv[q] = make_float4(o[0], o[1], o[2], o[3]);
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) at[q][c] = o[4 + c];
+                    }
+                }
+                TriSetup ts;
+                tri_setup(ts, sv);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    sm.ipx[q][it] = ts.px[q];
+                    sm.ipy[q][it] = ts.py[q];
+                    sm.inx[q][it] = ts.nx[q];
+                    sm.iny[q][it] = ts.ny[q];
+                    sm.iz[q][it] = ts.z[q];
+                    sm.iw[q][it] = ts.w[q];
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) sm.iat[q][c][it] = at[q][c];
+                }
+                sm.iinv[it] = ts.inv_area;
+                uint32_t bx0, bx1, by0, by1;
+                pixel_bbox(sv, W, H, bx0, bx1, by0, by1);
+                const uint32_t lx0 = max(bx0, X0) - X0, lx1 = min(bx1, X0 + TS) - X0;
+                const uint32_t ly0 = max(by0, Y0) - Y0, ly1 = min(by1, Y0 + TS) - Y0;
+                const bool nonempty = bx0 < bx1 && by0 < by1 && max(bx0, X0) < min(bx1, X0 + TS) &&
+                                      max(by0, Y0) < min(by1, Y0 + TS);
+                sm.irect[it] = nonempty ? (lx0 | (ly0 << 8) | (lx1 << 16) | (ly1 << 24)) : 0u;
+                sm.itri[it] = g;
+                sm.isub[it] = (uint16_t)k;
+                sm.idraw[it] = di;
+            }
+        }
+        __syncthreads();
+        const uint32_t nit = sm.misc[1];
+        // ---- B. candidate pixels per item (bbox clipped to the tile, row-major)
+        uint32_t ncand = 0;
+        if (threadIdx.x < nit) {
+            const uint32_t r = sm.irect[threadIdx.x];
+            ncand = (((r >> 16) & 0xFFu) - (r & 0xFFu)) * ((r >> 24) - ((r >> 8) & 0xFFu));
+        }
+        uint32_t P;
+        const uint32_t cex = block_excl_scan(ncand, sm.tmp, P);
+        if (threadIdx.x < nit) sm.ipfx[threadIdx.x] = cex;
+        if (threadIdx.x == 0) sm.ipfx[nit] = P;
+        __syncthreads();
+        // ---- C. coverage (EdgeFunctions::eval, mod.rs:134-146) and sample depths
+        // (RasterizerTriangle::fragment, mod.rs:225-253); fragments staged in order
+        uint32_t nfrag = 0;
+        for (uint32_t cb0 = 0; cb0 < P; cb0 += blockDim.x) {
+            const uint32_t k = cb0 + threadIdx.x;
+            uint32_t cov = 0, it = 0, pix = 0;
+            float z[S];
+#pragma unroll
+            for (int q = 0; q < S; ++q) z[q] = 0.0f;
+            if (k < P) {
+                uint32_t lo = 0, hi = nit;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (sm.ipfx[mid] <= k) lo = mid; else hi = mid;
+                }
+                it = lo;
+                const uint32_t r = sm.irect[it];
+                const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, w = ((r >> 16) & 0xFFu) - lx0;
+                const uint32_t rr = k - sm.ipfx[it];
+                const uint32_t lx = lx0 + rr % w, ly = ly0 + rr / w;
+                pix = ly * TS + lx;
+                const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
+                float e1s[S], e2s[S];
+#pragma unroll
+                for (int q = 0; q < S; ++q) {
+                    const float xs = fx + sample_dx<S>(q), ys = fy + sample_dy<S>(q);
+                    const float e0 = edge_eval(sm.inx[0][it], sm.iny[0][it], sm.ipx[0][it], sm.ipy[0][it], xs, ys);
+                    const float e1 = edge_eval(sm.inx[1][it], sm.iny[1][it], sm.ipx[1][it], sm.ipy[1][it], xs, ys);
+                    const float e2 = edge_eval(sm.inx[2][it], sm.iny[2][it], sm.ipx[2][it], sm.ipy[2][it], xs, ys);
+                    e1s[q] = e1;
+                    e2s[q] = e2;
+                    if (edge_pass(e0, sm.inx[0][it], sm.iny[0][it]) &&
+                        edge_pass(e1, sm.inx[1][it], sm.iny[1][it]) &&
+                        edge_pass(e2, sm.inx[2][it], sm.iny[2][it]))
+                        cov |= 1u << q;
+                }
+                if (cov) {
+                    const float inv = sm.iinv[it];
+#pragma unroll
+                    for (int q = 0; q < S; ++q)
+                        if ((cov >> q) & 1u)
+                            z[q] = interp_depth(e1s[q], e2s[q], inv, sm.iz[0][it], sm.iz[1][it], sm.iz[2][it]);
+                }
+            }
+            const bool flag = cov != 0;
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
+            const uint32_t warp = threadIdx.x >> 5;
+            if (lane_id() == 0) sm.tmp[warp] = __popc(bal);
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                const uint32_t nw = blockDim.x >> 5;
+                const uint32_t wc = threadIdx.x < nw ? sm.tmp[threadIdx.x] : 0u;
+                uint32_t x = wc;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (threadIdx.x >= (uint32_t)o) x += y;
+                }
+                sm.tmp[threadIdx.x] = x - wc;
+                if (threadIdx.x == 31) sm.tmp[32] = x;
+            }
+            __syncthreads();
+            const uint32_t rtot = sm.tmp[32];
+            const uint32_t pos = sm.tmp[warp] + __popc(bal & lanemask_lt());
+            __syncthreads();
+            if (nfrag + rtot > (uint32_t)C::FC) {
+                raster_flush<S, TS>(sm, nfrag, draws, s, X0, Y0, shaded, fsinv, oobc);
+                nfrag = 0;
+            }
+            if (flag) {
+                const uint32_t fi = nfrag + pos;
+                sm.fitem[fi] = (uint16_t)it;
+                sm.fpix[fi] = (uint16_t)pix;
+                sm.fcov[fi] = (uint8_t)cov;
+#pragma unroll
+                for (int q = 0; q < S; ++q) sm.fz[q][fi] = z[q];
+            }
+            nfrag += rtot;
+            __syncthreads();
+        }
+        if (nfrag) raster_flush<S, TS>(sm, nfrag, draws, s, X0, Y0, shaded, fsinv, oobc);
+        e0 += take;
+        __syncthreads();
+    }
+
+    // ---- resolve (resolve_and_clear + box_filter_color, mod.rs:478-518, buffers.rs:111-125)
+    for (uint32_t p = threadIdx.x; p < (uint32_t)C::NPIX; p += blockDim.x) {
+        const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
+        if (x >= W || y >= H) continue;
+        const unsigned long long o = (unsigned long long)y * W + x;
+        f.out[o] = box_filter<S>(&sm.cb[p * S]);
+        if (f.dbg_depth) {
+#pragma unroll
+            for (int q = 0; q < S; ++q) {
+                f.dbg_depth[o * S + q] = sm.zb[p * S + q];
+                f.dbg_color[o * S + q] = sm.cb[p * S + q];
+            }
+        }
+    }
+    // per-block statistics
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        sm.misc[2] = 0;
+        sm.misc[3] = 0;
+        sm.misc[4] = 0;
+    }
+    __syncthreads();
+    if (shaded) atomicAdd(&sm.misc[2], (uint32_t)shaded);
+    if (fsinv) atomicAdd(&sm.misc[3], (uint32_t)fsinv);
+    if (oobc) atomicAdd(&sm.misc[4], (uint32_t)oobc);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (sm.misc[2]) atomicAdd(&s.stats[STAT_SHADED], (unsigned long long)sm.misc[2]);
+        if (sm.misc[3]) atomicAdd(&s.stats[STAT_FSINV], (unsigned long long)sm.misc[3]);
+        if (sm.misc[4]) {
+            atomicAdd(&s.stats[STAT_OOB], (unsigned long long)sm.misc[4]);
+            atomicOr(s.status, ST_TEXTURE_OOB);
+        }
+    }
+}
+
+// ===================================================================== launchers
+
+template <int S, int TS>
+static cudaError_t launch_raster_t(const LaunchArgs& a) {
+    const size_t bytes = sizeof(RasterSmem<S, TS>);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_raster<S, TS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (a.raster_blocks == 0) return cudaSuccess;
+    k_raster<S, TS><<<a.raster_blocks, kRasterThreads, bytes, a.stream>>>(
+        a.raster_frames, a.raster_nframes, a.raster_tile_offset, a.draws, a.scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vertex(const LaunchArgs& a) {
+    if (a.vertex_blocks == 0) return cudaSuccess;
+    k_vertex<<<a.vertex_blocks, 256, 0, a.stream>>>(a.draws, a.frames, a.vblocks, a.scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_count(const LaunchArgs& a) {
+    if (a.nchunks == 0) return cudaSuccess;
+    static int configured = 0;
+    const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
+    if (bytes > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        configured = bytes;
+    }
+    k_bin_count<<<a.nchunks, 256, bytes, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scans(const LaunchArgs& a) {
+    if (a.scan_groups)
+        k_scan_cols<<<a.scan_groups, 1024, 0, a.stream>>>(a.frames, a.nframes, a.scratch);
+    if (a.nframes) k_scan_tiles<<<a.nframes, 1024, 0, a.stream>>>(a.frames, a.scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scatter(const LaunchArgs& a) {
+    if (a.nchunks == 0) return cudaSuccess;
+    static int configured = 0;
+    const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
+    if (bytes > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        configured = bytes;
+    }
+    k_bin_scatter<<<a.nchunks, kScatterThreads, bytes, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster(const LaunchArgs& a, int msaa, int ts) {
+    if (msaa == 4) {
+        if (ts == 8) return launch_raster_t<4, 8>(a);
+        if (ts == 16) return launch_raster_t<4, 16>(a);
+        if (ts == 32) return launch_raster_t<4, 32>(a);
+    } else if (msaa == 1) {
+        if (ts == 8) return launch_raster_t<1, 8>(a);
+        if (ts == 16) return launch_raster_t<1, 16>(a);
+        if (ts == 32) return launch_raster_t<1, 32>(a);
+    }
+    return cudaErrorInvalidValue;
+}
+
+size_t raster_smem(int msaa, int ts) {
+    if (msaa == 4) {
+        if (ts == 8) return raster_smem_bytes<4, 8>();
+        if (ts == 16) return raster_smem_bytes<4, 16>();
+        if (ts == 32) return raster_smem_bytes<4, 32>();
+    } else if (msaa == 1) {
+        if (ts == 8) return raster_smem_bytes<1, 8>();
+        if (ts == 16) return raster_smem_bytes<1, 16>();
+        if (ts == 32) return raster_smem_bytes<1, 32>();
+    }
+    return 0;
+}
+
+}  // namespace rast
+
+// ===================================================================== known-answer kernel
+
+namespace rast {
+
+// Evaluates one pipeline device function on caller-supplied inputs (single thread). Layouts
+// per op are documented beside rast_debug_kat in rast_api.cu.
+__global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned char* __restrict__ out) {
+    const float* fi = reinterpret_cast<const float*>(in);
+    float* fo = reinterpret_cast<float*>(out);
+    uint32_t* uo = reinterpret_cast<uint32_t*>(out);
+    const int32_t* ii = reinterpret_cast<const int32_t*>(in);
+    switch (op) {
+        case 0: {  // perspective divide of 3 clip vertices
+            for (int v = 0; v < 3; ++v) {
+                float4 n = persp_divide(make_float4(fi[4 * v], fi[4 * v + 1], fi[4 * v + 2], fi[4 * v + 3]));
+                fo[4 * v] = n.x; fo[4 * v + 1] = n.y; fo[4 * v + 2] = n.z; fo[4 * v + 3] = n.w;
+            }
+            break;
+        }
+        case 1: {  // viewport + setup: in {i32 w, i32 h, f32 ndc[12]}
+            const float* ndc = fi + 2;
+            float4 sv[3];
+            for (int v = 0; v < 3; ++v)
+                sv[v] = viewport(make_float4(ndc[4 * v], ndc[4 * v + 1], ndc[4 * v + 2], ndc[4 * v + 3]),
+                                 (float)ii[0], (float)ii[1]);
+            TriSetup t;
+            tri_setup(t, sv);
+            for (int v = 0; v < 3; ++v) {
+                fo[2 * v] = t.px[v]; fo[2 * v + 1] = t.py[v];
+                fo[6 + v] = t.z[v]; fo[9 + v] = t.w[v];
+                fo[13 + 2 * v] = t.nx[v]; fo[14 + 2 * v] = t.ny[v];
+            }
+            fo[12] = t.inv_area;
+            break;
+        }
+        case 2:    // fragment at pixel: in {f32 screen[9], i32 x, i32 y}; out {u32 mask, f32 d[4]}
+        case 4: {  // interpolate: in {screen[9], i32 x, i32 y, w[3], attrs[18]}; out attr[6]
+            float4 sv[3];
+            for (int v = 0; v < 3; ++v) sv[v] = make_float4(fi[3 * v], fi[3 * v + 1], fi[3 * v + 2], 1.0f);
+            const uint32_t x = (uint32_t)ii[9], y = (uint32_t)ii[10];
+            if (op == 4)
+                for (int v = 0; v < 3; ++v) sv[v].w = fi[11 + v];
+            TriSetup t;
+            tri_setup(t, sv);
+            uint32_t cov = 0;
+            float d[4] = {0, 0, 0, 0};
+            for (int q = 0; q < 4; ++q) {
+                const float xs = (float)x + sample_dx<4>(q), ys = (float)y + sample_dy<4>(q);
+                float e[3];
+                for (int k = 0; k < 3; ++k) e[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], xs, ys);
+                bool in3 = true;
+                for (int k = 0; k < 3; ++k) in3 = in3 && edge_pass(e[k], t.nx[k], t.ny[k]);
+                if (in3) {
+                    cov |= 1u << q;
+                    d[q] = interp_depth(e[1], e[2], t.inv_area, t.z[0], t.z[1], t.z[2]);
+                }
+            }
+            if (op == 2) {
+                uo[0] = cov;
+                for (int q = 0; q < 4; ++q) fo[1 + q] = d[q];
+            } else {
+                const float* at = fi + 14;
+                float xs, ys;
+                interp_point<4>(x, y, cov, xs, ys);
+                float e[3];
+                for (int k = 0; k < 3; ++k) e[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], xs, ys);
+                float u, v, w;
+                persp_bary(e[0], e[1], e[2], t.w[0], t.w[1], t.w[2], u, v, w);
+                for (int c = 0; c < 6; ++c) fo[c] = at[c] * u + at[6 + c] * v + at[12 + c] * w;
+            }
+            break;
+        }
+        case 3: {  // eval_single: in {screen[9], f32 x, f32 y}; out {e[3], u32 inside}
+            float4 sv[3];
+            for (int v = 0; v < 3; ++v) sv[v] = make_float4(fi[3 * v], fi[3 * v + 1], fi[3 * v + 2], 1.0f);
+            TriSetup t;
+            tri_setup(t, sv);
+            bool in3 = true;
+            for (int k = 0; k < 3; ++k) {
+                fo[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], fi[9], fi[10]);
+                in3 = in3 && edge_pass(fo[k], t.nx[k], t.ny[k]);
+            }
+            uo[3] = in3;
+            break;
+        }
+        case 5: {  // try_clip: in {verts[12], attrs[18]}; out {i32 result, i32 ntris, verts[ntris*12]}
+            ClipVert v3[3];
+            for (int v = 0; v < 3; ++v) {
+                for (int k = 0; k < 4; ++k) v3[v].p[k] = fi[4 * v + k];
+                for (int k = 0; k < 6; ++k) v3[v].a[k] = fi[12 + 6 * v + k];
+            }
+            uint32_t codes[3];
+            for (int v = 0; v < 3; ++v)
+                codes[v] = clip_code(make_float4(v3[v].p[0], v3[v].p[1], v3[v].p[2], v3[v].p[3]));
+            int cls = clip_classify(tri2x_area(v3[0].p[0], v3[0].p[1], v3[1].p[0], v3[1].p[1], v3[2].p[0], v3[2].p[1]),
+                                    codes[0], codes[1], codes[2]);
+            int32_t* io = reinterpret_cast<int32_t*>(out);
+            io[1] = 0;
+            if (cls == 2) {
+                ClipVert poly[kMaxPoly];
+                int n = clip_polygon(v3, poly);
+                if (n < 3) {
+                    cls = 0;
+                } else {
+                    io[1] = n - 2;
+                    for (int t = 0; t + 2 < n; ++t) {
+                        const ClipVert* tv[3] = {&poly[0], &poly[t + 1], &poly[t + 2]};
+                        for (int q = 0; q < 3; ++q)
+                            for (int k = 0; k < 4; ++k) fo[2 + (3 * t + q) * 4 + k] = tv[q]->p[k];
+                    }
+                }
+            }
+            io[0] = cls;
+            break;
+        }
+        case 6: {  // bbox (unclamped viewport 65535): in points[6]; out u64[4]
+            float4 sv[3];
+            for (int v = 0; v < 3; ++v) sv[v] = make_float4(fi[2 * v], fi[2 * v + 1], 0.0f, 1.0f);
+            uint32_t x0, x1, y0, y1;
+            pixel_bbox(sv, 0xFFFFu, 0xFFFFu, x0, x1, y0, y1);
+            unsigned long long* lo = reinterpret_cast<unsigned long long*>(out);
+            lo[0] = x0; lo[1] = x1; lo[2] = y0; lo[3] = y1;
+            break;
+        }
+        case 7: {  // box filter: in u32[4]; out u32
+            uo[0] = box_filter<4>(reinterpret_cast<const uint32_t*>(in));
+            break;
+        }
+        case 8: {  // to_argb: in rgba f32[4]; out u32
+            uo[0] = to_argb(fi[0], fi[1], fi[2], fi[3]);
+            break;
+        }
+        case 9: {  // texture sample: in {i32 w, i32 h, f32 u, f32 v, u32 texels[w*h]}; out {f32[4], u32 oob}
+            float inv255[256];
+            for (int b = 0; b < 256; ++b) inv255[b] = (float)b / 255.0f;
+            bool oob = false;
+            tex_sample(reinterpret_cast<const uint32_t*>(in) + 4, (uint32_t)ii[0], (uint32_t)ii[1], fi[2], fi[3],
+                       inv255, fo, oob);
+            uo[4] = oob;
+            break;
+        }
+        case 10: {  // Mat4 * Vec4: in {m[16], v[4]}; out f32[4]
+            for (int r = 0; r < 4; ++r) fo[r] = dot4(fi + 4 * r, fi[16], fi[17], fi[18], fi[19]);
+            break;
+        }
+        default:
+            break;
+    }
+}
+
+cudaError_t launch_kat(int op, const void* in, void* out, cudaStream_t stream) {
+    k_kat<<<1, 1, 0, stream>>>(op, static_cast<const unsigned char*>(in), static_cast<unsigned char*>(out));
+    return cudaGetLastError();
+}
+
+}  // namespace rast
