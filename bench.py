@@ -284,6 +284,7 @@ def run_ours(args):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * args.steps / e2e_s
+    queue()
     ref_img = r.framebuffer()
     assert (host_out.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
     h2d = npos.numel() * 4 + nuv.numel() * 4 + nidx.numel() * 4

@@ -442,10 +442,11 @@ rast_status rast_draw(rast_ctx* c, rast_mesh mesh, int vs_id, int fs_id) {
     if (!c || mesh >= c->meshes.size() || !c->meshes[mesh].live) return RAST_INVALID_ARG;
     if (vs_id != RAST_VS_MVP || fs_id < 0 || fs_id > 2) return RAST_INVALID_ARG;
     if (fs_id == RAST_FS_TEXTURE && c->textures.empty()) return RAST_INVALID_ARG;
+    // handles, not pointers: later uploads may reallocate the mesh table before the frame
     DrawJob d;
-    d.mesh = &c->meshes[mesh];
+    d.mesh = nullptr;
     d.mesh_id = mesh;
-    d.tex = c->textures.empty() ? nullptr : &c->textures[0];
+    d.tex = nullptr;
     d.fs = fs_id;
     float pv[16];
     mat4_mul(c->proj, c->view, pv);
@@ -481,6 +482,14 @@ static rast_status framebuffer_impl(rast_ctx* c, uint32_t* argb_out, bool sync) 
     J.dbg_depth = c->capture ? c->dbg_depth.p : nullptr;
     J.dbg_color = c->capture ? c->dbg_color.p : nullptr;
     J.draws = c->queue;
+    for (DrawJob& d : J.draws) {
+        if (d.mesh_id >= c->meshes.size() || !c->meshes[d.mesh_id].live) {
+            c->queue.clear();
+            return RAST_INVALID_ARG;
+        }
+        d.mesh = &c->meshes[d.mesh_id];
+        d.tex = c->textures.empty() ? nullptr : &c->textures[0];
+    }
     J.bin_hint = c->bin_hint;
     uint32_t nt = 0;
     for (const DrawJob& d : J.draws) nt += d.mesh->ntris;
