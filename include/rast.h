@@ -96,6 +96,27 @@ rast_status rast_framebuffer(rast_ctx* ctx, uint32_t* argb_out);
  * device pointer or NULL. Used by throughput loops; no counterpart in the reference. */
 rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out_device);
 
+/* One frame of one mesh that allocates nothing. No counterpart in the reference: it is for
+ * callers that cannot allocate device memory when they render (an engine or plugin host that
+ * owns all device memory through its own pool, or a loop that must not let cudaMalloc or
+ * cudaFree synchronise the device). The caller passes device pointers for the mesh (d_pos
+ * nverts*3, d_uv nverts*2, d_rgba nverts*4 or NULL, d_idx ntris*3 with every index < nverts),
+ * the RGBA8 texture (d_tex, one u32 per texel; needed for fs_id 0) and the width*height ARGB
+ * output, plus host row-major world/view/proj matrices. All intermediate buffers live in one
+ * 32 MiB array in device memory owned by the library and held on every GPU that loads it
+ * until exit; frames that need more, or more than 262144 vertices or triangles, return
+ * RAST_INVALID_ARG without launching anything. The first call on a device looks up that
+ * array's address (make it before any stream capture). Work runs on `stream`
+ * (cudaStream_t, NULL = legacy default) and the call waits for it to finish. Calls share the
+ * array: calls whose GPU work overlaps race and must be serialised by the caller. Same image,
+ * status and bit-exactness as rast_framebuffer for the same inputs. */
+rast_status rast_render_noalloc(int width, int height, int msaa, int tile, float clear_depth,
+                                const float* d_pos, const float* d_uv, const float* d_rgba,
+                                uint32_t nverts, const uint32_t* d_idx, uint32_t ntris,
+                                const float world[16], const float view[16], const float proj[16],
+                                const uint32_t* d_tex, int tex_w, int tex_h, int fs_id,
+                                uint32_t* d_argb, void* stream);
+
 /* Per-frame statistics of the last framebuffer call: samples written (popcount of
  * depth-passed masks), fragment-shader invocations, texel reads past the texture. */
 rast_status rast_stats(rast_ctx* ctx, uint64_t* shaded_samples, uint64_t* fs_invocations,

@@ -1,0 +1,68 @@
+"""rast_render_noalloc: one frame rendered with no device allocation by the library, for callers
+that must keep device memory allocation out of their render call (they hand in their own
+device buffers; the library's intermediates live in a fixed 32 MiB device array).
+
+The entry point is called twice in a row through the C ABI and each image is compared with the
+image of the ordinary entry point (rast_framebuffer) for the same scene; the tolerance is the
+one the parity tests use: bit-exact. This file is named so that pytest collects it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from rusterizer_gb300 import _lib, renderer, scenes
+
+pytestmark = pytest.mark.gpu
+
+fp = ctypes.POINTER(ctypes.c_float)
+
+
+def _dev(torch, a, dtype):
+    return torch.from_numpy(np.ascontiguousarray(a).view(dtype)).cuda()
+
+
+def _noalloc(torch, scene, out, tile=0):
+    d = scene["draws"][0]
+    pos = _dev(torch, d["pos"], np.float32)
+    uv = _dev(torch, d["uv"], np.float32)
+    rgba = _dev(torch, d["rgba"], np.float32)
+    idx = _dev(torch, d["idx"], np.int32)
+    tex = _dev(torch, scene["textures"][0].reshape(-1, 4).view(np.uint32).reshape(-1), np.int32)
+    th, tw = scene["textures"][0].shape[:2]
+    f = lambda m: np.ascontiguousarray(m, np.float32).ctypes.data_as(fp)  # noqa: E731
+    world, view, proj = (np.ascontiguousarray(m, np.float32) for m in (d["world"], scene["view"], scene["proj"]))
+    stream = torch.cuda.current_stream().cuda_stream
+    st = _lib.load().rast_render_noalloc(
+        scene["width"], scene["height"], scene["msaa"], tile, float(np.float32(scene["clear_depth"])),
+        ctypes.c_void_p(pos.data_ptr()), ctypes.c_void_p(uv.data_ptr()), ctypes.c_void_p(rgba.data_ptr()),
+        len(d["pos"]), ctypes.c_void_p(idx.data_ptr()), len(d["idx"]),
+        f(world), f(view), f(proj), ctypes.c_void_p(tex.data_ptr()), tw, th, int(d.get("fs", 0)),
+        ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream))
+    torch.cuda.synchronize()
+    return st
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.small_soup(7), lambda: scenes.config0()])
+def test_noalloc_matches_framebuffer_twice(make):
+    torch = pytest.importorskip("torch")
+    scene = make()
+    ref, st, r = renderer.render_scene(scene)
+    r.close()
+    assert st == _lib.OK
+    H, W = scene["height"], scene["width"]
+    out = torch.zeros(H * W, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        out.fill_(0)
+        assert _noalloc(torch, scene, out) == _lib.OK
+        img = out.cpu().numpy().view(np.uint32).reshape(H, W)
+        assert (img == ref).all()
+
+
+def test_noalloc_refuses_frames_beyond_its_scratch():
+    torch = pytest.importorskip("torch")
+    # 180k-triangle heightfield at 3840x2160: tile histograms, bins and the clip-polygon store
+    # need about 40 MB, more than the 32 MiB the entry point owns
+    scene = scenes.config2(n=300)
+    out = torch.zeros(16, dtype=torch.int32, device="cuda")
+    assert _noalloc(torch, scene, out) == _lib.INVALID_ARG
