@@ -455,12 +455,15 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 // ===================================================================== raster
 
 constexpr int kRasterThreads = 256;
+constexpr int kRasterWarps = kRasterThreads / 32;
 
 template <int S, int TS>
 struct RasterCfg {
     static constexpr int NPIX = TS * TS;
-    static constexpr int IC = 256;                 // items (triangles after clipping) per batch
-    static constexpr int FC = (TS >= 32) ? 512 : 768;  // fragments per flush
+    static constexpr int RW = TS / kRasterWarps;  // rows per warp: w, w + 8, w + 16, ...
+    static constexpr int IC = kRasterThreads;  // items (triangles after clipping) per batch
+    static constexpr int QC = 64;              // per-warp fragment ring
+    static_assert(TS % kRasterWarps == 0, "tile rows must split evenly over the warps");
 };
 
 template <int S, int TS>
@@ -468,26 +471,19 @@ struct RasterSmem {
     using C = RasterCfg<S, TS>;
     float zb[C::NPIX * S];
     uint32_t cb[C::NPIX * S];
-    // items (struct of arrays)
-    float ipx[3][C::IC], ipy[3][C::IC], inx[3][C::IC], iny[3][C::IC];
-    float iz[3][C::IC], iw[3][C::IC], iinv[C::IC];
-    float iat[3][6][C::IC];
-    uint32_t irect[C::IC];
+    // items of the current batch (struct of arrays)
+    float ipx[3][C::IC], ipy[3][C::IC], iz[3][C::IC], iw[3][C::IC], iinv[C::IC];
+    float iat[12][C::IC];  // uv (6 floats) or colour (12 floats), per the draw's shader
+    uint32_t irect[C::IC];  // tile-local pixel box: x0 | y0 << 8 | x1 << 16 | y1 << 24
     uint32_t itri[C::IC];
-    uint16_t isub[C::IC];
-    uint32_t idraw[C::IC];
-    uint32_t ipfx[C::IC + 1];
-    // fragments
-    float fz[S][C::FC];
-    uint16_t fitem[C::FC];
-    uint16_t fpix[C::FC];
-    uint16_t fslot[C::FC];
-    uint16_t plist[C::FC];
-    uint8_t fcov[C::FC];
-    uint8_t fdm[C::FC];
-    uint32_t pcnt[C::NPIX];
-    uint32_t poff[C::NPIX];
-    uint16_t lastw[C::NPIX * S];
+    uint32_t imeta[C::IC];  // draw << 8 | sub-triangle
+    uint32_t member[kRasterWarps][C::IC / 32];  // bit: item overlaps one of the warp's rows
+    uint16_t wlist[kRasterWarps][C::IC];         // the warp's items, in submission order
+    // per-warp rings of covered fragments, in submission order
+    float qz[kRasterWarps][S][C::QC];
+    uint16_t qitem[kRasterWarps][C::QC];
+    uint16_t qpix[kRasterWarps][C::QC];
+    uint8_t qcov[kRasterWarps][C::QC];
     float inv255[256];
     uint32_t tmp[40];
     uint32_t misc[8];
@@ -506,140 +502,122 @@ __device__ __forceinline__ uint32_t find_draw(const DrawDev* __restrict__ draws,
     return lo;
 }
 
-// Depth test in submission order for the staged fragments, then shading; see the per-step
-// comments. All threads of the block call this with the same nfrag.
+// Inward edge normal k of an item (RasterizerTriangle::new, src/rasterizer/mod.rs:199-204),
+// recomputed from the stored points with the same two subtractions.
 template <int S, int TS>
-__device__ void raster_flush(RasterSmem<S, TS>& sm, uint32_t nfrag, const DrawDev* __restrict__ draws,
-                             const Scratch& s, uint32_t X0, uint32_t Y0, unsigned long long& shaded,
-                             unsigned long long& fsinv, unsigned long long& oobc) {
+__device__ __forceinline__ void item_normal(const RasterSmem<S, TS>& sm, uint32_t it, int k, float& nx,
+                                            float& ny) {
+    const int n = k == 2 ? 0 : k + 1;
+    const float vx = sm.ipx[n][it] - sm.ipx[k][it];
+    const float vy = sm.ipy[n][it] - sm.ipy[k][it];
+    nx = -vy;
+    ny = vx;
+}
+
+// Depth test, shading and colour write of up to 32 queued fragments of one warp (lane = one
+// fragment, queue order = submission order). Fragments of the same pixel run in rounds of
+// increasing rank, so both the depth test (depth_coverage, src/rasterizer/mod.rs:363-378) and
+// the sample writes (write_pixel, mod.rs:380-397) happen in submission order.
+template <int S, int TS>
+__device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head,
+                                             uint32_t n, const DrawDev* __restrict__ draws,
+                                             const Scratch& s, uint32_t X0, uint32_t Y0,
+                                             uint32_t& shaded, uint32_t& fsinv, uint32_t& oobc) {
     using C = RasterCfg<S, TS>;
-    // 1. bucket fragments by pixel (arbitrary slot; restored to submission order in step 4)
-    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x)
-        sm.fslot[f] = (uint16_t)atomicAdd(&sm.pcnt[sm.fpix[f]], 1u);
-    __syncthreads();
-    // 2. pixel offsets: each thread scans a contiguous run of pixels
-    {
-        constexpr int PER = (C::NPIX + kRasterThreads - 1) / kRasterThreads;
-        const uint32_t a = threadIdx.x * PER;
-        uint32_t loc = 0;
+    const uint32_t lane = lane_id();
+    const bool valid = lane < n;
+    const uint32_t q = (head + lane) & (C::QC - 1);
+    uint32_t it = 0, pix = 0, cov = 0;
+    float z[S];
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (a + k < (uint32_t)C::NPIX) loc += sm.pcnt[a + k];
-        uint32_t total;
-        uint32_t run = block_excl_scan(loc, sm.tmp, total);
+    for (int k = 0; k < S; ++k) z[k] = 0.0f;
+    if (valid) {
+        it = sm.qitem[w][q];
+        pix = sm.qpix[w][q];
+        cov = sm.qcov[w][q];
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (a + k < (uint32_t)C::NPIX) {
-                sm.poff[a + k] = run;
-                run += sm.pcnt[a + k];
-            }
+        for (int k = 0; k < S; ++k) z[k] = sm.qz[w][k][q];
     }
-    __syncthreads();
-    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x)
-        sm.plist[sm.poff[sm.fpix[f]] + sm.fslot[f]] = (uint16_t)f;
-    __syncthreads();
-    // 3+4. per pixel, in submission order: depth_coverage (strict <, src/rasterizer/mod.rs:
-    // 363-378) then the depth writes of write_pixel (mod.rs:380-397); remember the last writer
-    // of each sample so that only its colour lands
-    for (uint32_t p = threadIdx.x; p < (uint32_t)C::NPIX; p += blockDim.x) {
-        const uint32_t c = sm.pcnt[p];
-        if (!c) continue;
-        const uint32_t o = sm.poff[p];
-        for (uint32_t j = 1; j < c; ++j) {  // insertion sort: fragment index = submission order
-            const uint16_t v = sm.plist[o + j];
-            uint32_t k = j;
-            while (k > 0 && sm.plist[o + k - 1] > v) {
-                sm.plist[o + k] = sm.plist[o + k - 1];
-                --k;
-            }
-            sm.plist[o + k] = v;
-        }
-        float z[S];
+    const uint32_t key = valid ? pix : 0x10000u + lane;
+    const uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t rank = __popc(grp & lanemask_lt());
+    const uint32_t maxr = __reduce_max_sync(0xFFFFFFFFu, rank);
+    uint32_t dm = 0;
+    for (uint32_t r = 0; r <= maxr; ++r) {
+        if (valid && rank == r) {
 #pragma unroll
-        for (int q = 0; q < S; ++q) z[q] = sm.zb[p * S + q];
-        for (uint32_t j = 0; j < c; ++j) {
-            const uint32_t f = sm.plist[o + j];
-            const uint32_t cov = sm.fcov[f];
-            uint32_t dm = 0;
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-                if ((cov >> q) & 1u) {
-                    const float fzq = sm.fz[q][f];
-                    if (fzq < z[q]) {
-                        dm |= 1u << q;
-                        z[q] = fzq;
-                        sm.lastw[p * S + q] = (uint16_t)f;
-                    }
+            for (int k = 0; k < S; ++k)
+                if (((cov >> k) & 1u) && z[k] < sm.zb[pix * S + k]) {
+                    dm |= 1u << k;
+                    sm.zb[pix * S + k] = z[k];
                 }
-            sm.fdm[f] = (uint8_t)dm;
             if (s.log) {
                 const unsigned long long slot = atomicAdd(s.log_n, 1ull);
                 if (slot < s.log_cap) {
-                    const uint32_t it = sm.fitem[f];
                     uint32_t* L = s.log + 4ull * slot;
                     L[0] = sm.itri[it];
-                    L[1] = sm.isub[it];
-                    L[2] = ((Y0 + p / TS) << 16) | (X0 + p % TS);
+                    L[1] = sm.imeta[it] & 0xFFu;
+                    L[2] = ((Y0 + pix / TS) << 16) | (X0 + pix % TS);
                     L[3] = (dm << 8) | cov;
                 } else {
                     atomicOr(s.status, ST_LOG_OVERFLOW);
                 }
             }
         }
-#pragma unroll
-        for (int q = 0; q < S; ++q) sm.zb[p * S + q] = z[q];
-        sm.pcnt[p] = 0;
+        __syncwarp();
     }
-    __syncthreads();
-    // 5. shading of every fragment that passed the depth test (Fragment::interpolate,
-    // mod.rs:69-100, then the fragment shader); colour lands where it is the last writer
-    for (uint32_t f = threadIdx.x; f < nfrag; f += blockDim.x) {
-        const uint32_t dm = sm.fdm[f];
-        if (!dm) continue;
-        const uint32_t it = sm.fitem[f];
-        const uint32_t p = sm.fpix[f];
-        const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
+    uint32_t argb = 0;
+    if (dm) {
+        // Fragment::interpolate (src/rasterizer/mod.rs:69-100), then the fragment shader
+        const uint32_t x = X0 + pix % TS, y = Y0 + pix / TS;
         float xs, ys;
         interp_point<S>(x, y, dm, xs, ys);
-        const float e0 = edge_eval(sm.inx[0][it], sm.iny[0][it], sm.ipx[0][it], sm.ipy[0][it], xs, ys);
-        const float e1 = edge_eval(sm.inx[1][it], sm.iny[1][it], sm.ipx[1][it], sm.ipy[1][it], xs, ys);
-        const float e2 = edge_eval(sm.inx[2][it], sm.iny[2][it], sm.ipx[2][it], sm.ipy[2][it], xs, ys);
-        float u, v, w;
-        persp_bary(e0, e1, e2, sm.iw[0][it], sm.iw[1][it], sm.iw[2][it], u, v, w);
-        const DrawDev& d = draws[sm.idraw[it]];
+        float e[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float nx, ny;
+            item_normal(sm, it, k, nx, ny);
+            e[k] = edge_eval(nx, ny, sm.ipx[k][it], sm.ipy[k][it], xs, ys);
+        }
+        float u, v, ww;
+        persp_bary(e[0], e[1], e[2], sm.iw[0][it], sm.iw[1][it], sm.iw[2][it], u, v, ww);
+        const DrawDev& d = draws[sm.imeta[it] >> 8];
         float col[4];
         if (d.fs == 0) {
             // FS::Texture (upstream src/main.rs:214-216)
-            const float tu = sm.iat[0][4][it] * u + sm.iat[1][4][it] * v + sm.iat[2][4][it] * w;
-            const float tv = sm.iat[0][5][it] * u + sm.iat[1][5][it] * v + sm.iat[2][5][it] * w;
+            const float tu = sm.iat[0][it] * u + sm.iat[2][it] * v + sm.iat[4][it] * ww;
+            const float tv = sm.iat[1][it] * u + sm.iat[3][it] * v + sm.iat[5][it] * ww;
             bool oob = false;
             tex_sample(d.tex, d.tex_w, d.tex_h, tu, tv, sm.inv255, col, oob);
             if (oob) ++oobc;
         } else if (d.fs == 1) {
             // FS::Color (upstream src/main.rs:217)
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                col[q] = sm.iat[0][q][it] * u + sm.iat[1][q][it] * v + sm.iat[2][q][it] * w;
+            for (int c = 0; c < 4; ++c)
+                col[c] = sm.iat[c][it] * u + sm.iat[4 + c][it] * v + sm.iat[8 + c][it] * ww;
         } else {
             // FS::Debug (upstream src/main.rs:218-220): grayscale(frag_coords.depths[0])
-            const float g = sm.fz[0][f];
-            col[0] = g;
-            col[1] = g;
-            col[2] = g;
+            col[0] = z[0];
+            col[1] = z[0];
+            col[2] = z[0];
             col[3] = 1.0f;
         }
-        const uint32_t argb = to_argb(col[0], col[1], col[2], col[3]);
-#pragma unroll
-        for (int q = 0; q < S; ++q)
-            if (((dm >> q) & 1u) && sm.lastw[p * S + q] == f) sm.cb[p * S + q] = argb;
+        argb = to_argb(col[0], col[1], col[2], col[3]);
         shaded += __popc(dm);
         fsinv += 1;
     }
-    __syncthreads();
+    for (uint32_t r = 0; r <= maxr; ++r) {
+        if (dm && rank == r) {
+#pragma unroll
+            for (int k = 0; k < S; ++k)
+                if ((dm >> k) & 1u) sm.cb[pix * S + k] = argb;
+        }
+        __syncwarp();
+    }
 }
 
 template <int S, int TS>
-__global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __restrict__ frames,
+__global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __restrict__ frames,
                                                            int nframes, uint32_t tile_offset,
                                                            const DrawDev* __restrict__ draws,
                                                            Scratch s) {
@@ -660,20 +638,20 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __res
     const uint32_t lt = gt - f.tile_begin;
     const uint32_t X0 = (lt % f.tiles_x) * TS, Y0 = (lt / f.tiles_x) * TS;
     const uint32_t W = f.width, H = f.height;
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
     for (uint32_t i = threadIdx.x; i < (uint32_t)(C::NPIX * S); i += blockDim.x) {
         sm.zb[i] = f.clear_depth;
         sm.cb[i] = kClearColor;
     }
-    for (uint32_t i = threadIdx.x; i < (uint32_t)C::NPIX; i += blockDim.x) sm.pcnt[i] = 0;
     sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
     __syncthreads();
-    unsigned long long shaded = 0, fsinv = 0, oobc = 0;
+    uint32_t shaded = 0, fsinv = 0, oobc = 0;
     const bool overflow = (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) != 0;
     const uint32_t nent = overflow ? 0u : s.tile_count[gt];
     const uint32_t* bins = s.bins + f.bin_base + (overflow ? 0u : s.tile_start[gt]);
 
     for (uint32_t e0 = 0; e0 < nent;) {
-        // ---- A. entries -> items (sub-triangles after clipping, in fan order)
+        // ---- A. entries -> items (sub-triangles after clipping, in fan order), one thread per entry
         const uint32_t e = e0 + threadIdx.x;
         uint32_t g = 0, aux = kNone, nitems = 0;
         if (e < nent) {
@@ -689,9 +667,10 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __res
         if (part) {
             const uint32_t di = find_draw(draws, f, g);
             const DrawDev& d = draws[di];
-            float4 sv[3];
+            const int fs = d.fs;
             for (uint32_t k = 0; k < nitems; ++k) {
                 const uint32_t it = iex + k;
+                float4 sv[3];
                 float at[3][6];
                 if (aux == kNone) {
                     const uint32_t tri = g - d.tbase;
@@ -700,15 +679,18 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __res
 #pragma unroll
                     for (int q = 0; q < 3; ++q) {
                         sv[q] = s.vscr[d.vbase + ii[q]];
-                        if (d.rgba) {
+                        if (fs == 1) {
+                            if (d.rgba) {
 #pragma unroll
-                            for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
-                        } else {
+                                for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
+                                for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
+                            }
+                        } else if (fs == 0) {
+                            at[q][4] = __ldg(d.uv + 2ull * ii[q]);
+                            at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
                         }
-                        at[q][4] = __ldg(d.uv + 2ull * ii[q]);
-                        at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
                     }
                 } else {
                     const float* st = s.clip_store + aux + 1;
@@ -721,126 +703,161 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __res
                         for (int c = 0; c < 6; ++c) at[q][c] = o[4 + c];
                     }
                 }
-                TriSetup ts;
-                tri_setup(ts, sv);
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    sm.ipx[q][it] = ts.px[q];
-                    sm.ipy[q][it] = ts.py[q];
-                    sm.inx[q][it] = ts.nx[q];
-                    sm.iny[q][it] = ts.ny[q];
-                    sm.iz[q][it] = ts.z[q];
-                    sm.iw[q][it] = ts.w[q];
+                    sm.ipx[q][it] = sv[q].x;
+                    sm.ipy[q][it] = sv[q].y;
+                    sm.iz[q][it] = sv[q].z;
+                    sm.iw[q][it] = sv[q].w;
+                    if (fs == 0) {
+                        sm.iat[2 * q][it] = at[q][4];
+                        sm.iat[2 * q + 1][it] = at[q][5];
+                    } else if (fs == 1) {
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) sm.iat[q][c][it] = at[q][c];
+                        for (int c = 0; c < 4; ++c) sm.iat[4 * q + c][it] = at[q][c];
+                    }
                 }
-                sm.iinv[it] = ts.inv_area;
+                // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
+                sm.iinv[it] = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
                 uint32_t bx0, bx1, by0, by1;
                 pixel_bbox(sv, W, H, bx0, bx1, by0, by1);
-                const uint32_t lx0 = max(bx0, X0) - X0, lx1 = min(bx1, X0 + TS) - X0;
-                const uint32_t ly0 = max(by0, Y0) - Y0, ly1 = min(by1, Y0 + TS) - Y0;
-                const bool nonempty = bx0 < bx1 && by0 < by1 && max(bx0, X0) < min(bx1, X0 + TS) &&
-                                      max(by0, Y0) < min(by1, Y0 + TS);
-                sm.irect[it] = nonempty ? (lx0 | (ly0 << 8) | (lx1 << 16) | (ly1 << 24)) : 0u;
+                const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
+                const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
+                const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1;
+                sm.irect[it] = nonempty ? ((cx0 - X0) | ((cy0 - Y0) << 8) | ((cx1 - X0) << 16) |
+                                           ((cy1 - Y0) << 24))
+                                        : 0u;
                 sm.itri[it] = g;
-                sm.isub[it] = (uint16_t)k;
-                sm.idraw[it] = di;
+                sm.imeta[it] = (di << 8) | k;
             }
         }
         __syncthreads();
         const uint32_t nit = sm.misc[1];
-        // ---- B. candidate pixels per item (bbox clipped to the tile, row-major)
-        uint32_t ncand = 0;
-        if (threadIdx.x < nit) {
-            const uint32_t r = sm.irect[threadIdx.x];
-            ncand = (((r >> 16) & 0xFFu) - (r & 0xFFu)) * ((r >> 24) - ((r >> 8) & 0xFFu));
+        // ---- B. which warps own a row of each item's box (warp w owns rows w, w+8, ...)
+        {
+            const uint32_t t = threadIdx.x;
+            uint32_t wm = 0;
+            if (t < nit) {
+                const uint32_t r = sm.irect[t];
+                const uint32_t ly0 = (r >> 8) & 0xFFu, ly1 = r >> 24;
+                if (ly1 > ly0) {
+                    const uint32_t nrow = ly1 - ly0;
+                    wm = nrow >= (uint32_t)kRasterWarps
+                             ? (1u << kRasterWarps) - 1u
+                             : (((1u << nrow) - 1u) << (ly0 % kRasterWarps));
+                    wm = (wm | (wm >> kRasterWarps)) & ((1u << kRasterWarps) - 1u);
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < kRasterWarps; ++w) {
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, (wm >> w) & 1u);
+                if (lane == 0) sm.member[w][warp] = bal;
+            }
         }
-        uint32_t P;
-        const uint32_t cex = block_excl_scan(ncand, sm.tmp, P);
-        if (threadIdx.x < nit) sm.ipfx[threadIdx.x] = cex;
-        if (threadIdx.x == 0) sm.ipfx[nit] = P;
         __syncthreads();
-        // ---- C. coverage (EdgeFunctions::eval, mod.rs:134-146) and sample depths
-        // (RasterizerTriangle::fragment, mod.rs:225-253); fragments staged in order
-        uint32_t nfrag = 0;
-        for (uint32_t cb0 = 0; cb0 < P; cb0 += blockDim.x) {
-            const uint32_t k = cb0 + threadIdx.x;
-            uint32_t cov = 0, it = 0, pix = 0;
-            float z[S];
+        // ---- C. per warp, in submission order: candidate pixels of its band, coverage
+        // (EdgeFunctions::eval, mod.rs:134-146), sample depths (RasterizerTriangle::fragment,
+        // mod.rs:225-253), then ordered depth test and shading of the covered fragments
+        uint32_t nmine = 0;
 #pragma unroll
-            for (int q = 0; q < S; ++q) z[q] = 0.0f;
-            if (k < P) {
-                uint32_t lo = 0, hi = nit;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (sm.ipfx[mid] <= k) lo = mid; else hi = mid;
-                }
-                it = lo;
-                const uint32_t r = sm.irect[it];
-                const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, w = ((r >> 16) & 0xFFu) - lx0;
-                const uint32_t rr = k - sm.ipfx[it];
-                const uint32_t lx = lx0 + rr % w, ly = ly0 + rr / w;
-                pix = ly * TS + lx;
-                const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
-                float e1s[S], e2s[S];
-#pragma unroll
-                for (int q = 0; q < S; ++q) {
-                    const float xs = fx + sample_dx<S>(q), ys = fy + sample_dy<S>(q);
-                    const float e0 = edge_eval(sm.inx[0][it], sm.iny[0][it], sm.ipx[0][it], sm.ipy[0][it], xs, ys);
-                    const float e1 = edge_eval(sm.inx[1][it], sm.iny[1][it], sm.ipx[1][it], sm.ipy[1][it], xs, ys);
-                    const float e2 = edge_eval(sm.inx[2][it], sm.iny[2][it], sm.ipx[2][it], sm.ipy[2][it], xs, ys);
-                    e1s[q] = e1;
-                    e2s[q] = e2;
-                    if (edge_pass(e0, sm.inx[0][it], sm.iny[0][it]) &&
-                        edge_pass(e1, sm.inx[1][it], sm.iny[1][it]) &&
-                        edge_pass(e2, sm.inx[2][it], sm.iny[2][it]))
-                        cov |= 1u << q;
-                }
-                if (cov) {
-                    const float inv = sm.iinv[it];
-#pragma unroll
-                    for (int q = 0; q < S; ++q)
-                        if ((cov >> q) & 1u)
-                            z[q] = interp_depth(e1s[q], e2s[q], inv, sm.iz[0][it], sm.iz[1][it], sm.iz[2][it]);
-                }
-            }
-            const bool flag = cov != 0;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
-            const uint32_t warp = threadIdx.x >> 5;
-            if (lane_id() == 0) sm.tmp[warp] = __popc(bal);
-            __syncthreads();
-            if (threadIdx.x < 32) {
-                const uint32_t nw = blockDim.x >> 5;
-                const uint32_t wc = threadIdx.x < nw ? sm.tmp[threadIdx.x] : 0u;
-                uint32_t x = wc;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                    if (threadIdx.x >= (uint32_t)o) x += y;
-                }
-                sm.tmp[threadIdx.x] = x - wc;
-                if (threadIdx.x == 31) sm.tmp[32] = x;
-            }
-            __syncthreads();
-            const uint32_t rtot = sm.tmp[32];
-            const uint32_t pos = sm.tmp[warp] + __popc(bal & lanemask_lt());
-            __syncthreads();
-            if (nfrag + rtot > (uint32_t)C::FC) {
-                raster_flush<S, TS>(sm, nfrag, draws, s, X0, Y0, shaded, fsinv, oobc);
-                nfrag = 0;
-            }
-            if (flag) {
-                const uint32_t fi = nfrag + pos;
-                sm.fitem[fi] = (uint16_t)it;
-                sm.fpix[fi] = (uint16_t)pix;
-                sm.fcov[fi] = (uint8_t)cov;
-#pragma unroll
-                for (int q = 0; q < S; ++q) sm.fz[q][fi] = z[q];
-            }
-            nfrag += rtot;
-            __syncthreads();
+        for (int src = 0; src < C::IC / 32; ++src) {
+            const uint32_t bits = sm.member[warp][src];
+            if ((bits >> lane) & 1u) sm.wlist[warp][nmine + __popc(bits & lanemask_lt())] = (uint16_t)(src * 32 + lane);
+            nmine += __popc(bits);
         }
-        if (nfrag) raster_flush<S, TS>(sm, nfrag, draws, s, X0, Y0, shaded, fsinv, oobc);
+        __syncwarp();
+        uint32_t head = 0, tail = 0;
+        for (uint32_t gb = 0; gb < nmine; gb += 32) {
+            const bool act = gb + lane < nmine;
+            const uint32_t it_l = act ? sm.wlist[warp][gb + lane] : 0u;
+            uint32_t cx0 = 0, cw = 1, cy0 = 0, c = 0;
+            if (act) {
+                const uint32_t r = sm.irect[it_l];
+                const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
+                // first row of the box owned by this warp, then every kRasterWarps-th row
+                const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
+                const uint32_t nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
+                cx0 = lx0;
+                cw = lx1 - lx0;
+                cy0 = first;
+                c = cw * nrows;
+            }
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            for (uint32_t pb = 0; pb < total; pb += 32) {
+                const uint32_t p = pb + lane;
+                // source lane: number of lanes whose inclusive count is <= p
+                uint32_t j = 0;
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1) {
+                    const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, j + st - 1);
+                    if (v <= p) j += st;
+                }
+                const uint32_t sj = min(j, 31u);
+                const uint32_t it = __shfl_sync(0xFFFFFFFFu, it_l, sj);
+                const uint32_t exc = __shfl_sync(0xFFFFFFFFu, incl - c, sj);
+                const uint32_t sx0 = __shfl_sync(0xFFFFFFFFu, cx0, sj);
+                const uint32_t sw = __shfl_sync(0xFFFFFFFFu, cw, sj);
+                const uint32_t sy0 = __shfl_sync(0xFFFFFFFFu, cy0, sj);
+                uint32_t cov = 0, pix = 0;
+                float z[S];
+#pragma unroll
+                for (int k = 0; k < S; ++k) z[k] = 0.0f;
+                if (p < total) {
+                    const uint32_t rr = p - exc;
+                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + kRasterWarps * (rr / sw);
+                    pix = ly * TS + lx;
+                    const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
+                    float n0x, n0y, n1x, n1y, n2x, n2y;
+                    item_normal(sm, it, 0, n0x, n0y);
+                    item_normal(sm, it, 1, n1x, n1y);
+                    item_normal(sm, it, 2, n2x, n2y);
+                    const float p0x = sm.ipx[0][it], p0y = sm.ipy[0][it];
+                    const float p1x = sm.ipx[1][it], p1y = sm.ipy[1][it];
+                    const float p2x = sm.ipx[2][it], p2y = sm.ipy[2][it];
+                    float e1s[S], e2s[S];
+#pragma unroll
+                    for (int k = 0; k < S; ++k) {
+                        const float xs = fx + sample_dx<S>(k), ys = fy + sample_dy<S>(k);
+                        const float e0 = edge_eval(n0x, n0y, p0x, p0y, xs, ys);
+                        const float e1 = edge_eval(n1x, n1y, p1x, p1y, xs, ys);
+                        const float e2 = edge_eval(n2x, n2y, p2x, p2y, xs, ys);
+                        e1s[k] = e1;
+                        e2s[k] = e2;
+                        if (edge_pass(e0, n0x, n0y) && edge_pass(e1, n1x, n1y) && edge_pass(e2, n2x, n2y))
+                            cov |= 1u << k;
+                    }
+                    if (cov) {
+                        const float inv = sm.iinv[it];
+                        const float z0 = sm.iz[0][it], z1 = sm.iz[1][it], z2 = sm.iz[2][it];
+#pragma unroll
+                        for (int k = 0; k < S; ++k)
+                            if ((cov >> k) & 1u) z[k] = interp_depth(e1s[k], e2s[k], inv, z0, z1, z2);
+                    }
+                }
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, cov != 0);
+                if (cov) {
+                    const uint32_t q = (tail + __popc(bal & lanemask_lt())) & (C::QC - 1);
+                    sm.qitem[warp][q] = (uint16_t)it;
+                    sm.qpix[warp][q] = (uint16_t)pix;
+                    sm.qcov[warp][q] = (uint8_t)cov;
+#pragma unroll
+                    for (int k = 0; k < S; ++k) sm.qz[warp][k][q] = z[k];
+                }
+                tail += __popc(bal);
+                __syncwarp();
+                if (tail - head >= 32) {
+                    warp_process<S, TS>(sm, warp, head, 32, draws, s, X0, Y0, shaded, fsinv, oobc);
+                    head += 32;
+                }
+            }
+        }
+        if (tail != head) warp_process<S, TS>(sm, warp, head, tail - head, draws, s, X0, Y0, shaded, fsinv, oobc);
         e0 += take;
         __syncthreads();
     }
@@ -860,16 +877,15 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameDev* __res
         }
     }
     // per-block statistics
-    __syncthreads();
     if (threadIdx.x == 0) {
         sm.misc[2] = 0;
         sm.misc[3] = 0;
         sm.misc[4] = 0;
     }
     __syncthreads();
-    if (shaded) atomicAdd(&sm.misc[2], (uint32_t)shaded);
-    if (fsinv) atomicAdd(&sm.misc[3], (uint32_t)fsinv);
-    if (oobc) atomicAdd(&sm.misc[4], (uint32_t)oobc);
+    if (shaded) atomicAdd(&sm.misc[2], shaded);
+    if (fsinv) atomicAdd(&sm.misc[3], fsinv);
+    if (oobc) atomicAdd(&sm.misc[4], oobc);
     __syncthreads();
     if (threadIdx.x == 0) {
         if (sm.misc[2]) atomicAdd(&s.stats[STAT_SHADED], (unsigned long long)sm.misc[2]);
