@@ -331,12 +331,104 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Config 3: 256 independent scenes (ntris log-uniform 100..200k, four resolutions, MSAA 1
+    or 4, own 512x512 texture) rendered as one CUDA-graph batch, against the same scenes rendered
+    one scene per launch sequence."""
+    import numpy as np
+    import torch
+
+    from rusterizer_gb300 import scenes
+    from rusterizer_gb300.batch import BatchRenderer
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    specs = scenes.batch_scene_specs(args.nscenes, 3)
+    sc = [scenes.batch_scene(s) for s in specs]
+    br = BatchRenderer()
+    for s in sc:
+        br.add_scene(s)
+    dev = [torch.empty(s["height"] * s["width"], dtype=torch.int32, device="cuda") for s in sc]
+    ptrs = [d.data_ptr() for d in dev]
+    tuned = br.autotune(ptrs)
+    g = br.capture(ptrs)
+    ext = torch.cuda.ExternalStream(BatchRenderer.graph_stream(g))
+    for _ in range(args.warmup):
+        BatchRenderer.replay(g)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(ext):
+                evs[k][0].record(ext)
+            BatchRenderer.replay(g, wait=False)
+            with torch.cuda.stream(ext):
+                evs[k][1].record(ext)
+        ext.synchronize()
+    batch_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(batch_ms)
+    value = world * len(sc) * args.steps / (total_ms / 1000.0)
+    # plain: one scene per launch sequence, synchronous, 256 calls
+    for i in range(len(sc)):
+        br.render([ptrs[i]], indices=[i])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(len(sc)):
+        br.render([ptrs[i]], indices=[i])
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_value = len(sc) / plain_s
+    # e2e: the whole batch through the public API with host outputs (device -> host copies)
+    host = [np.empty((s["height"], s["width"]), np.uint32) for s in sc]
+    br.render(host)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 4)):
+        br.render(host)
+    e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 4)
+    bytes_batch = sum(scenes.scene_bytes(s) for s in sc)
+    tris = sum(scenes.scene_triangles(s) for s in sc)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = bytes_batch / (total_ms / args.steps / 1000.0) / 1e9
+    cpu = None
+    if world == 1 and args.cpu_seconds > 0:
+        import oracle
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < args.cpu_seconds:
+            oracle.render_scene(sc[n % len(sc)], nthreads=1)
+            n += 1
+        dt = time.perf_counter() - t0
+        cpu = {"value": n / dt, "unit": "scenes/s", "cores": 1, "kind": "port",
+               "sample": f"first {n} scenes of the batch, single thread, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "scenes/s", "value": value, "unit": "scenes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"batched {len(sc)} scenes (config 3), CUDA graph",
+                       "config_index": 3, "triangles": tris, "autotune": tuned,
+                       "l2": "inputs (%.0f MB) larger than L2" % (bytes_batch / 1e6)},
+            "plain_scenes_per_s": plain_value, "batched_vs_plain": value / plain_value,
+            "roofline": {"bound": "hbm", "kernel": "whole batch", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": None, "algorithmic_bytes_per_step": bytes_batch},
+            "cpu_baseline": cpu,
+            "e2e": {"value": len(sc) / e2e_s, "unit": "scenes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(4 * s["width"] * s["height"] for s in sc))},
+            "gpu_launches": args.steps * (5 + 2 * 4),
+            "clocks": clk.summary(),
+        }), flush=True)
+    br.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3])
+    ap.add_argument("--nscenes", type=int, default=256)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -345,6 +437,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 3:
+        return run_batched(args)
     return run_ours(args)
 
 

@@ -117,6 +117,39 @@ rast_status rast_render_noalloc(int width, int height, int msaa, int tile, float
                                 const uint32_t* d_tex, int tex_w, int tex_h, int fs_id,
                                 uint32_t* d_argb, void* stream);
 
+/* ---- batched rendering (no counterpart in the reference: one Renderer draws one scene) ---- */
+
+/* One independent scene of a batch: one resident mesh, one fragment shader, its own target. */
+typedef struct rast_scene {
+    int width, height, msaa; /* msaa 1 or 4 */
+    int tile;                /* 8, 16 or 32; 0 = the context's autotuned choice */
+    float clear_depth;
+    rast_mesh mesh;
+    int texture;             /* texture slot used by RAST_FS_TEXTURE */
+    int fs_id;
+    float world[16], view[16], proj[16];
+    uint32_t* argb_out;      /* width*height ARGB: device pointer, or host pointer (copied back) */
+} rast_scene;
+
+/* Renders n scenes with one launch of each pipeline kernel for the whole batch; the raster
+ * kernel is persistent and takes tiles of all scenes from one queue, heaviest first. Same
+ * per-scene results as rendering each scene alone. Synchronous. */
+rast_status rast_render_batch(rast_ctx* ctx, const rast_scene* scenes, uint32_t n);
+
+/* Times tile sizes 8/16/32 for the MSAA-1 and MSAA-4 scenes of a batch and keeps the fastest
+ * pair in the context (used where rast_scene.tile == 0). best_tiles[0] = MSAA 1, [1] = MSAA 4. */
+rast_status rast_autotune_batch(rast_ctx* ctx, const rast_scene* scenes, uint32_t n,
+                                int best_tiles[2]);
+
+/* A batch captured into a CUDA graph once (after one sizing run) and re-rendered by one graph
+ * launch per call. argb_out pointers must be device pointers. The batch owns its own scratch
+ * and stream; the context's meshes and textures must outlive it. */
+typedef struct rast_batch rast_batch;
+rast_status rast_batch_create(rast_ctx* ctx, const rast_scene* scenes, uint32_t n, rast_batch** out);
+rast_status rast_batch_launch(rast_batch* batch, int wait);
+void* rast_batch_stream(rast_batch* batch);
+rast_status rast_batch_destroy(rast_batch* batch);
+
 /* Per-frame statistics of the last framebuffer call: samples written (popcount of
  * depth-passed masks), fragment-shader invocations, texel reads past the texture. */
 rast_status rast_stats(rast_ctx* ctx, uint64_t* shaded_samples, uint64_t* fs_invocations,

@@ -43,6 +43,12 @@ SIGNATURES = {
     "rast_framebuffer_async": (_i, [_vp, _vp]),
     "rast_render_noalloc": (_i, [_i, _i, _i, _i, _c.c_float, _vp, _vp, _vp, _u32, _vp, _u32,
                                  _fp, _fp, _fp, _vp, _i, _i, _i, _vp, _vp]),
+    "rast_render_batch": (_i, [_vp, _vp, _u32]),
+    "rast_autotune_batch": (_i, [_vp, _vp, _u32, _c.POINTER(_i)]),
+    "rast_batch_create": (_i, [_vp, _vp, _u32, _c.POINTER(_vp)]),
+    "rast_batch_launch": (_i, [_vp, _i]),
+    "rast_batch_stream": (_vp, [_vp]),
+    "rast_batch_destroy": (_i, [_vp]),
     "rast_stats": (_i, [_vp, _u64p, _u64p, _u64p]),
     "rast_stream": (_vp, [_vp]),
     "rast_set_profiling": (_i, [_vp, _i]),
@@ -53,6 +59,14 @@ SIGNATURES = {
     "rast_debug_log_read": (_i, [_vp, _u32p, _u64, _u64p]),
     "rast_debug_kat": (_i, [_i, _vp, _c.c_size_t, _vp, _c.c_size_t]),
 }
+
+class Scene(ctypes.Structure):
+    """struct rast_scene (include/rast.h)."""
+    _fields_ = [("width", _c.c_int), ("height", _c.c_int), ("msaa", _c.c_int), ("tile", _c.c_int),
+                ("clear_depth", _c.c_float), ("mesh", _c.c_uint32), ("texture", _c.c_int),
+                ("fs_id", _c.c_int), ("world", _c.c_float * 16), ("view", _c.c_float * 16),
+                ("proj", _c.c_float * 16), ("argb_out", _c.c_void_p)]
+
 
 _lib = None
 

@@ -150,7 +150,8 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         bool ok = E.vclip.reserve(vtot) && E.vscr.reserve(vtot) && E.vcode.reserve(vtot) &&
                   E.tri_rect.reserve(ttot) && E.tri_aux.reserve(ttot) &&
                   E.counts.reserve(count_tot) && E.tile_start.reserve(tile_tot) &&
-                  E.tile_count.reserve(tile_tot) && E.bins.reserve(bin_tot) &&
+                  E.tile_count.reserve(tile_tot) && E.tile_order.reserve(tile_tot) &&
+                  E.bins.reserve(bin_tot) &&
                   E.clip_store.reserve(std::max<uint64_t>(clip_est, E.clip_hint)) &&
                   E.frame_need.reserve(frames.size());
         if (!ok) return RAST_OOM;
@@ -207,6 +208,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         S.counts = E.counts.p;
         S.tile_start = E.tile_start.p;
         S.tile_count = E.tile_count.p;
+        S.tile_order = E.tile_order.p;
         S.bins = E.bins.p;
         S.clip_store = E.clip_store.p;
         S.clip_cap = E.clip_store.cap;
@@ -229,7 +231,12 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         if (err == cudaSuccess) err = launch_bin_scatter(a);
         if (E.profiling) cudaEventRecord(E.ev[4], st);
         // raster: one launch per (msaa, tile) group of consecutive frames
-        for (size_t i = 0; i < frames.size() && err == cudaSuccess;) {
+        int group = 0;
+        for (size_t i = 0; i < frames.size() && err == cudaSuccess; ++group) {
+            if (group >= 8) {
+                err = cudaErrorInvalidValue;
+                break;
+            }
             size_t j = i;
             uint32_t blocks = 0;
             while (j < frames.size() && frames[j].msaa == frames[i].msaa && frames[j].ts == frames[i].ts) {
@@ -240,6 +247,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
             a.raster_nframes = (int)(j - i);
             a.raster_tile_offset = frames[i].tile_begin;
             a.raster_blocks = blocks;
+            a.raster_queue = &E.d_state->queue[4 * group];
             err = launch_raster(a, frames[i].msaa, frames[i].ts);
             i = j;
         }
@@ -254,6 +262,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                                 cudaMemcpyDeviceToHost, st);
             }
             if (cudaStreamSynchronize(st) != cudaSuccess) return RAST_CUDA_ERROR;
+            E.desc_pending = false;  // the stream drained: the staging buffer is free
             const uint32_t status = E.h_state->status;
             bool retry = false;
             if (status & ST_BIN_OVERFLOW) {
@@ -285,22 +294,6 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
 }  // namespace rast
 
 // ============================================================================ C ABI
-
-struct rast_ctx {
-    Engine E;
-    int width = 0, height = 0, msaa = 4;
-    float clear_depth = 3.40282347e+38f;
-    int tile_req = 0;
-    std::vector<MeshRec> meshes;
-    std::vector<TexRec> textures;
-    float world[16], view[16], proj[16];
-    std::vector<DrawJob> queue;
-    DevBuf<uint32_t> out;
-    bool capture = false;
-    DevBuf<float> dbg_depth;
-    DevBuf<uint32_t> dbg_color;
-    uint64_t bin_hint = 0;
-};
 
 static void identity16(float* m) {
     for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0f : 0.0f;

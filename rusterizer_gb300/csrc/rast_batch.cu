@@ -1,0 +1,271 @@
+// rast_batch.cu - many independent scenes per launch sequence, CUDA-graph capture of a fixed
+// batch, and the tile-size autotuner.
+//
+// A batch is a list of frames handed to run_frames at once: the vertex, binning and scan
+// kernels run once over every scene, and the persistent raster kernel (one launch per
+// (MSAA, tile size) class) takes tiles of all scenes from a single queue, heaviest first, so
+// uneven scenes share the GPU instead of each occupying it for a launch of its own. Scenes are
+// independent, so each scene's image is bit-identical to rendering it alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/rast.h"
+#include "rast_internal.h"
+
+using namespace rast;
+
+namespace {
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes attr;
+    const bool dev = cudaPointerGetAttributes(&attr, p) == cudaSuccess &&
+                     (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    return dev;
+}
+
+int scene_tile(const rast_ctx* c, const rast_scene& s) {
+    int req = s.tile;
+    if (req == 0) req = c->tuned_tile[s.msaa == 4 ? 1 : 0];
+    return choose_tile(s.width, s.height, s.msaa, req);
+}
+
+// Validates the scenes and turns them into frame jobs. Host outputs (when allowed) are
+// redirected to `staging` at the returned offsets.
+rast_status build_jobs(rast_ctx* c, const rast_scene* sc, uint32_t n, bool allow_host_out,
+                       std::vector<FrameJob>& jobs, std::vector<size_t>* host_off, size_t* staging_px) {
+    jobs.clear();
+    jobs.resize(n);
+    size_t px = 0;
+    if (host_off) host_off->assign(n, (size_t)-1);
+    for (uint32_t i = 0; i < n; ++i) {
+        const rast_scene& s = sc[i];
+        if (s.width < 1 || s.height < 1 || s.width > 16384 || s.height > 16384 ||
+            (s.msaa != 1 && s.msaa != 4) || s.fs_id < 0 || s.fs_id > 2 || !s.argb_out)
+            return RAST_INVALID_ARG;
+        if (s.mesh >= c->meshes.size() || !c->meshes[s.mesh].live) return RAST_INVALID_ARG;
+        if (s.fs_id == RAST_FS_TEXTURE && (s.texture < 0 || s.texture >= (int)c->textures.size()))
+            return RAST_INVALID_ARG;
+        const int ts = scene_tile(c, s);
+        if (!ts) return RAST_INVALID_ARG;
+        FrameJob& J = jobs[i];
+        J.width = s.width;
+        J.height = s.height;
+        J.msaa = s.msaa;
+        J.ts = ts;
+        J.clear_depth = s.clear_depth;
+        if (is_device_ptr(s.argb_out)) {
+            J.out_dev = s.argb_out;
+        } else {
+            if (!allow_host_out) return RAST_INVALID_ARG;
+            (*host_off)[i] = px;
+            px += (size_t)s.width * (size_t)s.height;
+        }
+        DrawJob d;
+        d.mesh = &c->meshes[s.mesh];
+        d.mesh_id = s.mesh;
+        d.tex = (s.texture >= 0 && s.texture < (int)c->textures.size()) ? &c->textures[s.texture] : nullptr;
+        d.fs = s.fs_id;
+        float pv[16];
+        mat4_mul(s.proj, s.view, pv);
+        mat4_mul(pv, s.world, d.mvp);
+        J.draws.assign(1, d);
+        J.ntris_hint = d.mesh->ntris;
+        if (c->batch_hints.size() == n) J.bin_hint = c->batch_hints[i];
+    }
+    if (staging_px) *staging_px = px;
+    return RAST_OK;
+}
+
+rast_status render_jobs(rast_ctx* c, const rast_scene* sc, uint32_t n, std::vector<FrameJob>& jobs,
+                        const std::vector<size_t>& host_off, size_t staging_px) {
+    if (staging_px && !c->batch_out.reserve(staging_px)) return RAST_OOM;
+    for (uint32_t i = 0; i < n; ++i)
+        if (host_off[i] != (size_t)-1) jobs[i].out_dev = c->batch_out.p + host_off[i];
+    c->E.sync_after = true;
+    rast_status st = run_frames(c->E, jobs);
+    if (st != RAST_OK && st != RAST_TEXTURE_OOB) return st;
+    c->batch_hints.resize(n);
+    for (uint32_t i = 0; i < n; ++i)
+        c->batch_hints[i] = std::max<uint64_t>(c->batch_hints[i], jobs[i].need + jobs[i].need / 8);
+    bool copied = false;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (host_off[i] == (size_t)-1) continue;
+        const size_t bytes = (size_t)sc[i].width * sc[i].height * sizeof(uint32_t);
+        if (cudaMemcpyAsync(sc[i].argb_out, c->batch_out.p + host_off[i], bytes, cudaMemcpyDeviceToHost,
+                            c->E.stream) != cudaSuccess)
+            return RAST_CUDA_ERROR;
+        copied = true;
+    }
+    if (copied && cudaStreamSynchronize(c->E.stream) != cudaSuccess) return RAST_CUDA_ERROR;
+    return st;
+}
+
+}  // namespace
+
+struct rast_batch {
+    rast_ctx* ctx = nullptr;
+    Engine E;
+    std::vector<FrameJob> jobs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+rast_status rast_render_batch(rast_ctx* c, const rast_scene* sc, uint32_t n) {
+    if (!c || (n && !sc)) return RAST_INVALID_ARG;
+    if (n == 0) return RAST_OK;
+    std::vector<FrameJob> jobs;
+    std::vector<size_t> host_off;
+    size_t staging = 0;
+    rast_status st = build_jobs(c, sc, n, true, jobs, &host_off, &staging);
+    if (st != RAST_OK) return st;
+    return render_jobs(c, sc, n, jobs, host_off, staging);
+}
+
+rast_status rast_autotune_batch(rast_ctx* c, const rast_scene* sc, uint32_t n, int best_tiles[2]) {
+    if (!c || !sc || n == 0) return RAST_INVALID_ARG;
+    bool has1 = false, has4 = false;
+    for (uint32_t i = 0; i < n; ++i) (sc[i].msaa == 4 ? has4 : has1) = true;
+    const int sizes[3] = {8, 16, 32};
+    std::vector<rast_scene> trial(sc, sc + n);
+    // every trial writes into the staging buffer, not the caller's images
+    size_t px = 0;
+    for (uint32_t i = 0; i < n; ++i) px += (size_t)sc[i].width * sc[i].height;
+    if (!c->batch_out.reserve(px)) return RAST_OOM;
+    float best_ms = 3.0e38f;
+    int best1 = 0, best4 = 0;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return RAST_CUDA_ERROR;
+    rast_status result = RAST_OK;
+    const int saved[2] = {c->tuned_tile[0], c->tuned_tile[1]};
+    for (int a = 0; a < (has1 ? 3 : 1) && result == RAST_OK; ++a)
+        for (int b = 0; b < (has4 ? 3 : 1) && result == RAST_OK; ++b) {
+            const int t1 = has1 ? sizes[a] : 0, t4 = has4 ? sizes[b] : 0;
+            size_t off = 0;
+            for (uint32_t i = 0; i < n; ++i) {
+                trial[i] = sc[i];
+                trial[i].tile = 0;
+                trial[i].argb_out = c->batch_out.p + off;
+                off += (size_t)sc[i].width * sc[i].height;
+            }
+            c->tuned_tile[0] = t1;
+            c->tuned_tile[1] = t4;
+            std::vector<FrameJob> jobs;
+            float ms = 0.0f;
+            for (int rep = 0; rep < 3 && result == RAST_OK; ++rep) {
+                rast_status st = build_jobs(c, trial.data(), n, false, jobs, nullptr, nullptr);
+                if (st != RAST_OK) {
+                    result = st;
+                    break;
+                }
+                c->E.sync_after = true;
+                cudaEventRecord(e0, c->E.stream);
+                st = run_frames(c->E, jobs);
+                cudaEventRecord(e1, c->E.stream);
+                cudaEventSynchronize(e1);
+                if (st != RAST_OK && st != RAST_TEXTURE_OOB) {
+                    result = st;
+                    break;
+                }
+                c->batch_hints.resize(n);
+                for (uint32_t i = 0; i < n; ++i)
+                    c->batch_hints[i] = std::max<uint64_t>(c->batch_hints[i], jobs[i].need + jobs[i].need / 8);
+                float t = 0.0f;
+                cudaEventElapsedTime(&t, e0, e1);
+                if (rep > 0) ms += t;  // the first run sizes buffers
+            }
+            if (result == RAST_OK && ms < best_ms) {
+                best_ms = ms;
+                best1 = t1;
+                best4 = t4;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (result != RAST_OK) {
+        c->tuned_tile[0] = saved[0];
+        c->tuned_tile[1] = saved[1];
+        return result;
+    }
+    c->tuned_tile[0] = best1;
+    c->tuned_tile[1] = best4;
+    if (best_tiles) {
+        best_tiles[0] = best1;
+        best_tiles[1] = best4;
+    }
+    return RAST_OK;
+}
+
+rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, rast_batch** out) {
+    if (!c || !sc || n == 0 || !out) return RAST_INVALID_ARG;
+    rast_batch* b = new (std::nothrow) rast_batch();
+    if (!b) return RAST_OOM;
+    b->ctx = c;
+    rast_status st = build_jobs(c, sc, n, false, b->jobs, nullptr, nullptr);
+    if (st == RAST_OK && !b->E.init()) st = RAST_CUDA_ERROR;
+    if (st == RAST_OK) {
+        // one synchronous run sizes every buffer of this batch's own engine
+        b->E.sync_after = true;
+        st = run_frames(b->E, b->jobs);
+        if (st == RAST_TEXTURE_OOB) st = RAST_OK;
+    }
+    if (st == RAST_OK) {
+        for (FrameJob& J : b->jobs) J.bin_hint = std::max<uint64_t>(J.bin_hint, J.need);
+        b->E.sync_after = false;
+        if (cudaStreamBeginCapture(b->E.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            st = RAST_CUDA_ERROR;
+        } else {
+            rast_status rs = run_frames(b->E, b->jobs);
+            cudaMemcpyAsync(b->E.h_state, b->E.d_state, sizeof(DeviceState), cudaMemcpyDeviceToHost,
+                            b->E.stream);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(b->E.stream, &g);
+            if (rs != RAST_OK || ce != cudaSuccess || !g) {
+                st = rs != RAST_OK ? rs : RAST_CUDA_ERROR;
+                if (g) cudaGraphDestroy(g);
+            } else {
+                b->graph = g;
+                if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) st = RAST_CUDA_ERROR;
+            }
+        }
+        cudaGetLastError();
+    }
+    if (st != RAST_OK) {
+        rast_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return RAST_OK;
+}
+
+rast_status rast_batch_launch(rast_batch* b, int wait) {
+    if (!b || !b->exec) return RAST_INVALID_ARG;
+    if (cudaGraphLaunch(b->exec, b->E.stream) != cudaSuccess) return RAST_CUDA_ERROR;
+    if (!wait) return RAST_OK;
+    if (cudaStreamSynchronize(b->E.stream) != cudaSuccess) return RAST_CUDA_ERROR;
+    const uint32_t s = b->E.h_state->status;
+    if (s & (ST_BIN_OVERFLOW | ST_CLIP_STORE_OVERFLOW)) return RAST_BIN_OVERFLOW;
+    if (s & ST_CLIP_OVERFLOW) return RAST_CLIP_OVERFLOW;
+    if (s & ST_TEXTURE_OOB) return RAST_TEXTURE_OOB;
+    return RAST_OK;
+}
+
+void* rast_batch_stream(rast_batch* b) { return b ? (void*)b->E.stream : nullptr; }
+
+rast_status rast_batch_destroy(rast_batch* b) {
+    if (!b) return RAST_INVALID_ARG;
+    if (b->E.stream) cudaStreamSynchronize(b->E.stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    delete b;
+    return RAST_OK;
+}
+
+}  // extern "C"

@@ -174,6 +174,7 @@ struct DeviceState {
     unsigned long long stats[STAT_COUNT];
     unsigned long long clip_used;
     unsigned long long log_n;
+    unsigned int queue[32];  // raster tile queues, 4 counters per (msaa, tile) group
 };
 
 struct Engine {
@@ -181,7 +182,7 @@ struct Engine {
     DevBuf<float4> vclip, vscr;
     DevBuf<uint16_t> vcode;
     DevBuf<unsigned long long> tri_rect;
-    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, bins;
+    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, tile_order, bins;
     DevBuf<float> clip_store;
     DevBuf<unsigned long long> frame_need;
     DevBuf<uint32_t> log;
@@ -234,3 +235,24 @@ int choose_tile(int w, int h, int msaa, int req);
 rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs);
 
 }  // namespace rast
+
+// The context behind the C ABI: resident meshes and textures, the plain path's draw queue and
+// framebuffer, and the tile sizes chosen by the batch autotuner.
+struct rast_ctx {
+    rast::Engine E;
+    int width = 0, height = 0, msaa = 4;
+    float clear_depth = 3.40282347e+38f;
+    int tile_req = 0;
+    std::vector<rast::MeshRec> meshes;
+    std::vector<rast::TexRec> textures;
+    float world[16], view[16], proj[16];
+    std::vector<rast::DrawJob> queue;
+    rast::DevBuf<uint32_t> out;
+    bool capture = false;
+    rast::DevBuf<float> dbg_depth;
+    rast::DevBuf<uint32_t> dbg_color;
+    uint64_t bin_hint = 0;
+    int tuned_tile[2] = {0, 0};             // batch autotuner: MSAA 1, MSAA 4
+    std::vector<uint64_t> batch_hints;      // bins needed per scene by the last batch
+    rast::DevBuf<uint32_t> batch_out;       // staging for host-pointer batch outputs
+};

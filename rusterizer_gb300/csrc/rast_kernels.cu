@@ -502,6 +502,16 @@ __device__ __forceinline__ uint32_t find_draw(const DrawDev* __restrict__ draws,
     return lo;
 }
 
+__device__ __forceinline__ uint32_t frame_of_tile(const FrameDev* __restrict__ frames, int nframes,
+                                                  uint32_t gt) {
+    int lo = 0, hi = nframes;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (frames[mid].tile_begin <= gt) lo = mid; else hi = mid;
+    }
+    return (uint32_t)lo;
+}
+
 // Inward edge normal k of an item (RasterizerTriangle::new, src/rasterizer/mod.rs:199-204),
 // recomputed from the stored points with the same two subtractions.
 template <int S, int TS>
@@ -618,37 +628,39 @@ __device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, 
 
 template <int S, int TS>
 __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __restrict__ frames,
-                                                           int nframes, uint32_t tile_offset,
+                                                           int nframes,
+                                                           const uint32_t* __restrict__ order,
+                                                           uint32_t ntotal,
+                                                           unsigned int* __restrict__ queue,
                                                            const DrawDev* __restrict__ draws,
                                                            Scratch s) {
     using C = RasterCfg<S, TS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterSmem<S, TS>& sm = *reinterpret_cast<RasterSmem<S, TS>*>(smem_raw);
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = nframes;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (frames[mid].tile_begin <= tile_offset + blockIdx.x) lo = mid; else hi = mid;
-        }
-        sm.misc[0] = (uint32_t)lo;
-    }
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+    sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
+    uint32_t shaded = 0, fsinv = 0, oobc = 0;
+    const uint32_t nbusy = *(volatile unsigned int*)&queue[2];  // written by k_tile_order
+
+    // persistent loop over the tiles that have entries, heaviest first
+    for (;;) {
+    if (threadIdx.x == 0) sm.misc[0] = atomicAdd(&queue[0], 1u);
     __syncthreads();
-    const FrameDev& f = frames[sm.misc[0]];
-    const uint32_t gt = tile_offset + blockIdx.x;
+    const uint32_t qi = sm.misc[0];
+    __syncthreads();
+    if (qi >= nbusy) break;
+    const uint32_t gt = order[qi];
+    const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
     const uint32_t lt = gt - f.tile_begin;
     const uint32_t X0 = (lt % f.tiles_x) * TS, Y0 = (lt / f.tiles_x) * TS;
     const uint32_t W = f.width, H = f.height;
-    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
     for (uint32_t i = threadIdx.x; i < (uint32_t)(C::NPIX * S); i += blockDim.x) {
         sm.zb[i] = f.clear_depth;
         sm.cb[i] = kClearColor;
     }
-    sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
     __syncthreads();
-    uint32_t shaded = 0, fsinv = 0, oobc = 0;
-    const bool overflow = (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) != 0;
-    const uint32_t nent = overflow ? 0u : s.tile_count[gt];
-    const uint32_t* bins = s.bins + f.bin_base + (overflow ? 0u : s.tile_start[gt]);
+    const uint32_t nent = s.tile_count[gt];
+    const uint32_t* bins = s.bins + f.bin_base + s.tile_start[gt];
 
     for (uint32_t e0 = 0; e0 < nent;) {
         // ---- A. entries -> items (sub-triangles after clipping, in fan order), one thread per entry
@@ -876,7 +888,35 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             }
         }
     }
+    }  // tiles with entries
+
+    // ---- tiles without entries: warps take whole tiles independently and write the resolve
+    // of clear samples (the clear colour)
+    for (;;) {
+        uint32_t qi = 0;
+        if (lane == 0) qi = atomicAdd(&queue[1], 1u);
+        qi = __shfl_sync(0xFFFFFFFFu, qi, 0) + nbusy;
+        if (qi >= ntotal) break;
+        const uint32_t gt = order[qi];
+        const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
+        const uint32_t lt = gt - f.tile_begin;
+        const uint32_t x0 = (lt % f.tiles_x) * TS, y0 = (lt / f.tiles_x) * TS;
+        for (uint32_t i = lane; i < (uint32_t)C::NPIX; i += 32) {
+            const uint32_t x = x0 + i % TS, y = y0 + i / TS;
+            if (x >= f.width || y >= f.height) continue;
+            const unsigned long long o = (unsigned long long)y * f.width + x;
+            f.out[o] = kClearColor;
+            if (f.dbg_depth) {
+#pragma unroll
+                for (int q = 0; q < S; ++q) {
+                    f.dbg_depth[o * S + q] = f.clear_depth;
+                    f.dbg_color[o * S + q] = kClearColor;
+                }
+            }
+        }
+    }
     // per-block statistics
+    __syncthreads();
     if (threadIdx.x == 0) {
         sm.misc[2] = 0;
         sm.misc[3] = 0;
@@ -897,21 +937,64 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
     }
 }
 
+// Tile queue of one raster launch: tiles with entries first, in decreasing order of entry
+// count (bucketed by bit length), then tiles without entries; queue[2] = tiles with entries.
+// One block.
+__global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
+                                                     const uint32_t* __restrict__ tile_count,
+                                                     uint32_t* __restrict__ order,
+                                                     unsigned int* __restrict__ queue,
+                                                     const uint32_t* __restrict__ status) {
+    __shared__ uint32_t cnt[33], off[33];
+    if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    // after a bin overflow every tile is cleared and the host re-runs the frame
+    const bool overflow = (*(volatile const uint32_t*)status & ST_BIN_OVERFLOW) != 0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t c = overflow ? 0u : tile_count[tile0 + i];
+        atomicAdd(&cnt[32 - __clz(c)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int b = 32; b >= 0; --b) {
+            off[b] = run;
+            run += cnt[b];
+        }
+        queue[2] = n - cnt[0];
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t c = overflow ? 0u : tile_count[tile0 + i];
+        const uint32_t pos = atomicAdd(&off[32 - __clz(c)], 1u);
+        order[tile0 + pos] = tile0 + i;
+    }
+}
+
 // ===================================================================== launchers
 
 template <int S, int TS>
 static cudaError_t launch_raster_t(const LaunchArgs& a) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
-    static bool configured = false;
-    if (!configured) {
+    static int grid_cap = 0;
+    if (!grid_cap) {
         cudaError_t e = cudaFuncSetAttribute(k_raster<S, TS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
-        configured = true;
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<S, TS>, kRasterThreads, bytes);
+        if (e != cudaSuccess) return e;
+        grid_cap = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
-    k_raster<S, TS><<<a.raster_blocks, kRasterThreads, bytes, a.stream>>>(
-        a.raster_frames, a.raster_nframes, a.raster_tile_offset, a.draws, a.scratch);
+    k_tile_order<<<1, 1024, 0, a.stream>>>(a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
+                                           a.scratch.tile_order, a.raster_queue, a.scratch.status);
+    const unsigned grid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
+    k_raster<S, TS><<<grid, kRasterThreads, bytes, a.stream>>>(
+        a.raster_frames, a.raster_nframes, a.scratch.tile_order + a.raster_tile_offset, a.raster_blocks,
+        a.raster_queue, a.draws, a.scratch);
     return cudaGetLastError();
 }
 

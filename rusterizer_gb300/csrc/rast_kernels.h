@@ -24,7 +24,8 @@ struct LaunchArgs {
     const FrameDev* raster_frames;
     int raster_nframes;
     uint32_t raster_tile_offset;
-    uint32_t raster_blocks;
+    uint32_t raster_blocks;        // tiles in the group
+    unsigned int* raster_queue;    // the group's 4 tile-queue counters (zeroed per frame)
     Scratch scratch;
 };
 

@@ -146,6 +146,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     const size_t o_counts = c.take(sizeof(uint32_t) * (size_t)nchunks * F.ntiles);
     const size_t o_tstart = c.take(sizeof(uint32_t) * F.ntiles);
     const size_t o_tcount = c.take(sizeof(uint32_t) * F.ntiles);
+    const size_t o_torder = c.take(sizeof(uint32_t) * F.ntiles);
     const size_t o_need = c.take(sizeof(unsigned long long));
     const size_t o_bins = c.take(sizeof(uint32_t) * F.bin_cap);
     const size_t clip_floats = 32ull * ntris + 4096ull;
@@ -197,6 +198,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     a.raster_nframes = 1;
     a.raster_tile_offset = 0;
     a.raster_blocks = F.ntiles;
+    a.raster_queue = dstate->queue;
     Scratch& S = a.scratch;
     S.vclip = reinterpret_cast<float4*>(base + o_vclip);
     S.vscr = reinterpret_cast<float4*>(base + o_vscr);
@@ -206,6 +208,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     S.counts = reinterpret_cast<uint32_t*>(base + o_counts);
     S.tile_start = reinterpret_cast<uint32_t*>(base + o_tstart);
     S.tile_count = reinterpret_cast<uint32_t*>(base + o_tcount);
+    S.tile_order = reinterpret_cast<uint32_t*>(base + o_torder);
     S.bins = reinterpret_cast<uint32_t*>(base + o_bins);
     S.clip_store = reinterpret_cast<float*>(base + o_clip);
     S.clip_cap = clip_floats;

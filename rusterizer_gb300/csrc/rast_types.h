@@ -94,6 +94,7 @@ struct Scratch {
     uint32_t* counts;
     uint32_t* tile_start;
     uint32_t* tile_count;
+    uint32_t* tile_order;               // raster queue: tiles by decreasing entry count
     uint32_t* bins;
     float* clip_store;
     unsigned long long clip_cap;        // floats
