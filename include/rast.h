@@ -150,6 +150,38 @@ rast_status rast_batch_launch(rast_batch* batch, int wait);
 void* rast_batch_stream(rast_batch* batch);
 rast_status rast_batch_destroy(rast_batch* batch);
 
+/* ---- serving (no counterpart in the reference) --------------------------------------------
+ * A dispatcher thread renders submitted scenes with continuous batching: whenever one of
+ * `streams` launch slots is free, every queued request that fits the HBM budget (and
+ * max_batch) goes into one batched launch, so requests that arrive while others run are
+ * admitted as slots and memory free up, and two batches can overlap on the device. Meshes and
+ * textures stay resident in the context (upload them before creating the server and do not
+ * change them while it runs). one_per_launch = 1 gives the plain server (one request per
+ * launch) for comparison. */
+typedef struct rast_server rast_server;
+typedef struct rast_server_config {
+    uint64_t hbm_budget_bytes; /* in-flight scratch + image bytes admitted at once (0 = 40 GB) */
+    uint32_t max_batch;        /* scenes per launch (0 = no limit) */
+    int streams;               /* batches in flight at once, 1 or 2 */
+    int one_per_launch;        /* 1: plain server, one request per launch */
+} rast_server_config;
+
+rast_status rast_server_create(rast_ctx* ctx, const rast_server_config* cfg, rast_server** out);
+/* Queues one scene (argb_out: device or pinned host pointer). RAST_ADMISSION_REFUSED when the
+ * scene alone exceeds the budget. Thread-safe. */
+rast_status rast_server_submit(rast_server* srv, const rast_scene* scene, uint64_t* request_id);
+/* RAST_NOT_READY until the request has finished; then its status, and latency from submit to
+ * completion in ms. */
+rast_status rast_server_poll(rast_server* srv, uint64_t request_id, double* latency_ms);
+/* Waits up to timeout_ms (negative = no limit) for the request; RAST_TIMEOUT when it expires. */
+rast_status rast_server_wait(rast_server* srv, uint64_t request_id, int timeout_ms, double* latency_ms);
+/* Latency percentiles and throughput over the requests completed since the last reset. */
+rast_status rast_server_stats(rast_server* srv, double* p50_ms, double* p99_ms, uint64_t* completed,
+                              double* requests_per_s, double* mean_batch);
+rast_status rast_server_reset_stats(rast_server* srv);
+/* Drains the queue and stops the dispatcher. */
+rast_status rast_server_destroy(rast_server* srv);
+
 /* Per-frame statistics of the last framebuffer call: samples written (popcount of
  * depth-passed masks), fragment-shader invocations, texel reads past the texture. */
 rast_status rast_stats(rast_ctx* ctx, uint64_t* shaded_samples, uint64_t* fs_invocations,

@@ -49,6 +49,14 @@ SIGNATURES = {
     "rast_batch_launch": (_i, [_vp, _i]),
     "rast_batch_stream": (_vp, [_vp]),
     "rast_batch_destroy": (_i, [_vp]),
+    "rast_server_create": (_i, [_vp, _vp, _c.POINTER(_vp)]),
+    "rast_server_submit": (_i, [_vp, _vp, _u64p]),
+    "rast_server_poll": (_i, [_vp, _u64, _c.POINTER(_c.c_double)]),
+    "rast_server_wait": (_i, [_vp, _u64, _i, _c.POINTER(_c.c_double)]),
+    "rast_server_stats": (_i, [_vp, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double), _u64p,
+                               _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
+    "rast_server_reset_stats": (_i, [_vp]),
+    "rast_server_destroy": (_i, [_vp]),
     "rast_stats": (_i, [_vp, _u64p, _u64p, _u64p]),
     "rast_stream": (_vp, [_vp]),
     "rast_set_profiling": (_i, [_vp, _i]),
@@ -66,6 +74,12 @@ class Scene(ctypes.Structure):
                 ("clear_depth", _c.c_float), ("mesh", _c.c_uint32), ("texture", _c.c_int),
                 ("fs_id", _c.c_int), ("world", _c.c_float * 16), ("view", _c.c_float * 16),
                 ("proj", _c.c_float * 16), ("argb_out", _c.c_void_p)]
+
+
+class ServerConfig(ctypes.Structure):
+    """struct rast_server_config (include/rast.h)."""
+    _fields_ = [("hbm_budget_bytes", _c.c_uint64), ("max_batch", _c.c_uint32), ("streams", _c.c_int),
+                ("one_per_launch", _c.c_int)]
 
 
 _lib = None

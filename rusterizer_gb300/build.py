@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "librast.so")
-SOURCES = ["rast_kernels.cu", "rast_api.cu", "rast_noalloc.cu", "rast_batch.cu"]
+SOURCES = ["rast_kernels.cu", "rast_api.cu", "rast_noalloc.cu", "rast_batch.cu", "rast_server.cu"]
 HEADERS = ["rast_device.cuh", "rast_types.h", "rast_kernels.h", "rast_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true",

@@ -65,6 +65,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         if (jobs[a].msaa != jobs[b].msaa) return jobs[a].msaa < jobs[b].msaa;
         return jobs[a].ts < jobs[b].ts;
     });
+    E.h_order = order;
 
     for (int attempt = 0; attempt < 3; ++attempt) {
         std::vector<FrameDev>& frames = E.h_frames;

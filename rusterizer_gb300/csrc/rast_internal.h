@@ -204,6 +204,7 @@ struct Engine {
     std::vector<ChunkDev> h_chunks;
     std::vector<uint2> h_vblocks;
     std::vector<unsigned char> h_scratch;
+    std::vector<size_t> h_order;  // job index of each frame of the last launch (device order)
     cudaEvent_t desc_done = nullptr;  // last descriptor upload finished reading h_desc
     bool desc_pending = false, desc_valid = false;
     size_t desc_bytes = 0;

@@ -1,0 +1,81 @@
+"""Render server: requests submitted concurrently are batched on the device, and every result
+is identical to the same scene rendered alone (and to the oracle)."""
+import numpy as np
+import pytest
+
+import oracle
+from rusterizer_gb300 import _lib, scenes
+from rusterizer_gb300.batch import BatchRenderer
+from rusterizer_gb300.server import RenderServer
+
+pytestmark = pytest.mark.gpu
+
+
+def pool():
+    specs = scenes.batch_scene_specs(12, seed=44, min_tris=50, max_tris=4000)
+    return [scenes.batch_scene((n, min(w, 512), min(h, 384), m, s)) for n, w, h, m, s in specs]
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain"])
+def test_server_results_same_alone_and_in_the_mix(mode):
+    torch = pytest.importorskip("torch")
+    sc = pool()
+    br = BatchRenderer()
+    for s in sc:
+        br.add_scene(s)
+    alone = []
+    for i, s in enumerate(sc):
+        img = np.zeros((s["height"], s["width"]), np.uint32)
+        br.render([img], indices=[i])
+        alone.append(img)
+    srv = RenderServer(br, streams=2, one_per_launch=(mode == "plain"))
+    outs, rids = [], []
+    for rep in range(3):
+        for i, s in enumerate(sc):
+            o = torch.zeros(s["height"] * s["width"], dtype=torch.int32, device="cuda")
+            outs.append((i, o))
+            rids.append(srv.submit(i, o.data_ptr()))
+    for rid in rids:
+        st, lat = srv.wait(rid, timeout_ms=60000)
+        assert st in (_lib.OK, _lib.TEXTURE_OOB), st
+        assert lat >= 0.0
+    for i, o in outs:
+        s = sc[i]
+        img = o.cpu().numpy().view(np.uint32).reshape(s["height"], s["width"])
+        assert (img == alone[i]).all(), (mode, s["name"])
+    for i in range(0, len(sc), 4):
+        ref, *_ = oracle.render_scene(sc[i])
+        assert (alone[i] == ref).all()
+    st = srv.stats()
+    assert st["completed"] == len(rids)
+    if mode == "plain":
+        assert st["mean_batch"] == 1.0
+    srv.close()
+    br.close()
+
+
+def test_server_admission_budget():
+    torch = pytest.importorskip("torch")
+    sc = pool()[:4]
+    br = BatchRenderer()
+    for s in sc:
+        br.add_scene(s)
+    # a budget below one scene's footprint refuses it outright
+    tiny = RenderServer(br, budget_bytes=1024)
+    o = torch.zeros(sc[0]["height"] * sc[0]["width"], dtype=torch.int32, device="cuda")
+    with pytest.raises(_lib.RastError) as e:
+        tiny.submit(0, o.data_ptr())
+    assert e.value.status == _lib.ADMISSION_REFUSED
+    tiny.close()
+    # a budget that fits only a few scenes at a time still completes everything
+    one = RenderServer(br, budget_bytes=6 << 20, streams=2)
+    outs = [torch.zeros(s["height"] * s["width"], dtype=torch.int32, device="cuda") for s in sc]
+    rids = [one.submit(i, outs[i].data_ptr()) for i in range(len(sc))]
+    for rid in rids:
+        assert one.wait(rid, timeout_ms=60000)[0] in (_lib.OK, _lib.TEXTURE_OOB)
+    for i, s in enumerate(sc):
+        ref = np.zeros((s["height"], s["width"]), np.uint32)
+        br.render([ref], indices=[i])
+        assert (outs[i].cpu().numpy().view(np.uint32).reshape(ref.shape) == ref).all()
+    one.close()
+    br.close()
