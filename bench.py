@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
            1: "triangle soup 100k tris 1920x1080 4xMSAA",
            2: "heightfield 2M tris 3840x2160 4xMSAA"}
-LAUNCHES_PER_FRAME = 6  # vertex, bin count, column scan, tile scan, scatter, raster
+LAUNCHES_PER_FRAME = 7  # vertex, bin count, column scan, tile scan, scatter, tile order, raster
 
 
 def make_scene(cfg):
@@ -415,7 +415,10 @@ def run_batched(args):
             "cpu_baseline": cpu,
             "e2e": {"value": len(sc) / e2e_s, "unit": "scenes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(4 * s["width"] * s["height"] for s in sc))},
-            "gpu_launches": args.steps * (5 + 2 * 4),
+            # per replay: vertex, bin count, two scans, scatter, then tile order + raster for
+            # each (MSAA, tile size) group the batch holds
+            "gpu_launches": args.steps * (5 + 2 * len({(s.get("msaa", 4), tuned.get(
+                "msaa%d_tile" % s.get("msaa", 4), 0)) for s in sc})),
             "clocks": clk.summary(),
         }), flush=True)
     br.close()

@@ -57,7 +57,7 @@ void rast_destroy(rast_ctx* ctx);
 
 /* Depth clear value; the reference uses f32::MAX (src/rasterizer/buffers.rs:6). */
 rast_status rast_set_clear_depth(rast_ctx* ctx, float depth);
-/* Screen tile edge in pixels (8, 16, 32 or 64); 0 selects automatically. */
+/* Screen tile edge in pixels (8, 16 or 32); 0 selects automatically. */
 rast_status rast_set_tile_size(rast_ctx* ctx, int tile);
 
 /* Upload a mesh (Mesh{vertices, indices, attributes}, src/mesh.rs:5-12) so that it stays
@@ -70,7 +70,9 @@ rast_status rast_mesh_upload(rast_ctx* ctx, const float* pos, const float* uv, c
 rast_status rast_mesh_free(rast_ctx* ctx, rast_mesh mesh);
 /* Overwrite a resident mesh with new host data of the same vertex and triangle counts (the
  * reference borrows the mesh afresh on every render call, src/render.rs:98-110); copies only,
- * no allocation. rgba must be given iff the mesh was uploaded with colours. */
+ * no allocation. rgba must be given iff the mesh was uploaded with colours. The indices are
+ * checked on the device, not here: a triangle with an index >= nverts is skipped and the
+ * next rast_framebuffer returns RAST_INVALID_ARG. */
 rast_status rast_mesh_update(rast_ctx* ctx, rast_mesh mesh, const float* pos, const float* uv,
                              const float* rgba, const uint32_t* idx);
 
@@ -100,7 +102,8 @@ rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out_device);
  * callers that cannot allocate device memory when they render (an engine or plugin host that
  * owns all device memory through its own pool, or a loop that must not let cudaMalloc or
  * cudaFree synchronise the device). The caller passes device pointers for the mesh (d_pos
- * nverts*3, d_uv nverts*2, d_rgba nverts*4 or NULL, d_idx ntris*3 with every index < nverts),
+ * nverts*3, d_uv nverts*2, d_rgba nverts*4 or NULL, d_idx ntris*3; a triangle with an index
+ * >= nverts is skipped on the device and the call returns RAST_INVALID_ARG),
  * the RGBA8 texture (d_tex, one u32 per texel; needed for fs_id 0) and the width*height ARGB
  * output, plus host row-major world/view/proj matrices. All intermediate buffers live in one
  * 32 MiB array in device memory owned by the library and held on every GPU that loads it

@@ -284,6 +284,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
             std::memcpy(E.last_stats, E.h_state->stats, sizeof(E.last_stats));
             if (status & ST_BIN_OVERFLOW) return RAST_BIN_OVERFLOW;
             if (status & ST_CLIP_STORE_OVERFLOW) return RAST_BIN_OVERFLOW;
+            if (status & ST_BAD_INDEX) return RAST_INVALID_ARG;
             if (status & ST_CLIP_OVERFLOW) return RAST_CLIP_OVERFLOW;
             if (status & ST_TEXTURE_OOB) return RAST_TEXTURE_OOB;
         }
@@ -398,8 +399,6 @@ rast_status rast_mesh_update(rast_ctx* c, rast_mesh mesh, const float* pos, cons
     MeshRec& m = c->meshes[mesh];
     if ((m.nverts && (!pos || !uv)) || (m.ntris && !idx) || ((rgba != nullptr) != (m.rgba != nullptr)))
         return RAST_INVALID_ARG;
-    for (uint64_t i = 0; i < 3ull * m.ntris; ++i)
-        if (idx[i] >= m.nverts) return RAST_INVALID_ARG;
     cudaStream_t st = c->E.stream;
     bool ok = true;
     if (m.nverts) {

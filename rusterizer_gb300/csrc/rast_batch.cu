@@ -252,6 +252,7 @@ rast_status rast_batch_launch(rast_batch* b, int wait) {
     if (cudaStreamSynchronize(b->E.stream) != cudaSuccess) return RAST_CUDA_ERROR;
     const uint32_t s = b->E.h_state->status;
     if (s & (ST_BIN_OVERFLOW | ST_CLIP_STORE_OVERFLOW)) return RAST_BIN_OVERFLOW;
+    if (s & ST_BAD_INDEX) return RAST_INVALID_ARG;
     if (s & ST_CLIP_OVERFLOW) return RAST_CLIP_OVERFLOW;
     if (s & ST_TEXTURE_OOB) return RAST_TEXTURE_OOB;
     return RAST_OK;

@@ -146,6 +146,12 @@ __device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t 
     aux = kNone;
     const uint32_t i0 = __ldg(d.idx + 3ull * tri), i1 = __ldg(d.idx + 3ull * tri + 1),
                    i2 = __ldg(d.idx + 3ull * tri + 2);
+    // primitive_assembly indexes the vertex list (src/render.rs:75-96) and panics past its end;
+    // here the triangle is skipped and the frame reports an invalid argument
+    if (i0 >= d.nverts || i1 >= d.nverts || i2 >= d.nverts) {
+        atomicOr(s.status, ST_BAD_INDEX);
+        return;
+    }
     const uint32_t v[3] = {d.vbase + i0, d.vbase + i1, d.vbase + i2};
     const float4 c0 = s.vclip[v[0]], c1 = s.vclip[v[1]], c2 = s.vclip[v[2]];
     const int cls = clip_classify(tri2x_area(c0.x, c0.y, c1.x, c1.y, c2.x, c2.y), s.vcode[v[0]],

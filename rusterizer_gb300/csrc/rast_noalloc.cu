@@ -236,6 +236,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
         return RAST_CUDA_ERROR;
     }
     if (h.status & (ST_BIN_OVERFLOW | ST_CLIP_STORE_OVERFLOW)) return RAST_BIN_OVERFLOW;
+    if (h.status & ST_BAD_INDEX) return RAST_INVALID_ARG;
     if (h.status & ST_CLIP_OVERFLOW) return RAST_CLIP_OVERFLOW;
     if (h.status & ST_TEXTURE_OOB) return RAST_TEXTURE_OOB;
     return RAST_OK;

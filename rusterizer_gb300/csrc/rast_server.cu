@@ -187,7 +187,8 @@ struct rast_server {
             return;
         }
         rast_status rs = RAST_OK;
-        if (status & ST_CLIP_OVERFLOW) rs = RAST_CLIP_OVERFLOW;
+        if (status & ST_BAD_INDEX) rs = RAST_INVALID_ARG;
+        else if (status & ST_CLIP_OVERFLOW) rs = RAST_CLIP_OVERFLOW;
         else if (status & ST_TEXTURE_OOB) rs = RAST_TEXTURE_OOB;
         for (uint64_t id : sl.ids) {
             Request& r = reqs[id];

@@ -33,6 +33,7 @@ enum StatusBits : uint32_t {
     ST_CLIP_OVERFLOW = 1u << 2,
     ST_CLIP_STORE_OVERFLOW = 1u << 3,
     ST_LOG_OVERFLOW = 1u << 4,
+    ST_BAD_INDEX = 1u << 5,  // a vertex index >= the mesh's vertex count (triangle skipped)
 };
 
 enum StatSlots : int {

@@ -156,6 +156,17 @@ class Renderer:
         self._meshes[key] = (h.value, orig)  # keeps the object, and so its id, alive
         return h.value
 
+    def update(self, mesh, pos, uv, idx, rgba=None):
+        """Overwrite an uploaded mesh's data in place (same counts). Indices are checked on the
+        device: an out-of-range index makes the next framebuffer() raise INVALID_ARG."""
+        h = self.upload(mesh)
+        pos = np.ascontiguousarray(pos, np.float32)
+        uv = np.ascontiguousarray(uv, np.float32)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        rg = None if rgba is None else np.ascontiguousarray(rgba, np.float32).ctypes.data_as(_fp)
+        check(_lib.load().rast_mesh_update(self._ctx, h, pos.ctypes.data_as(_fp), uv.ctypes.data_as(_fp),
+                                           rg, idx.ctypes.data_as(_u32p)), "mesh update")
+
     def render(self, mesh, vertex_shader=VS_MVP, fragment_shader=FS_TEXTURE):
         """Renderer::render (src/render.rs:98-114): queue the mesh with the current uniforms."""
         L = _lib.load()

@@ -140,3 +140,32 @@ def test_repeated_frames_same_result():
     a2, _, _ = renderer.render_scene(s, renderer=r)
     r.close()
     assert (a1 == a2).all()
+
+
+def test_out_of_range_index_detected_on_device():
+    """primitive_assembly panics on an index past the vertex list (src/render.rs:75-96); here
+    the device skips that triangle and the frame reports INVALID_ARG, and the next frame with
+    valid indices is bit-exact again."""
+    from rusterizer_gb300 import _lib, renderer
+    import oracle
+    s = scenes.small_soup(71)
+    d = s["draws"][0]
+    r = renderer.Renderer(s["width"], s["height"], s.get("msaa", 4))
+    r.set_clear_depth(s.get("clear_depth", FLT_MAX))
+    for i, t in enumerate(s["textures"]):
+        r.uniforms().bind_texture(i, renderer.Texture(t))
+    blk = r.uniforms().write_block()
+    blk.view, blk.projection, blk.world = s["view"], s["proj"], d["world"]
+    bad = np.array(d["idx"], np.uint32).copy()
+    bad.reshape(-1)[5] = len(d["pos"])  # one past the end
+    r.update(d, d["pos"], d["uv"], bad)
+    r.render(d, renderer.VS_MVP, d.get("fs", 0))
+    with pytest.raises(_lib.RastError) as e:
+        r.framebuffer()
+    assert e.value.status == _lib.INVALID_ARG
+    r.update(d, d["pos"], d["uv"], d["idx"])
+    r.render(d, renderer.VS_MVP, d.get("fs", 0))
+    img = r.framebuffer()
+    ref, *_ = oracle.render_scene(s)
+    assert (img == ref).all()
+    r.close()

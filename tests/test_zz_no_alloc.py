@@ -66,3 +66,23 @@ def test_noalloc_refuses_frames_beyond_its_scratch():
     scene = scenes.config2(n=300)
     out = torch.zeros(16, dtype=torch.int32, device="cuda")
     assert _noalloc(torch, scene, out) == _lib.INVALID_ARG
+
+
+def test_noalloc_out_of_range_index_reported():
+    """Indices live in the caller's device memory, so the check runs on the device: the
+    triangle is skipped and the call returns INVALID_ARG; a following valid call is exact."""
+    torch = pytest.importorskip("torch")
+    scene = scenes.small_soup(9)
+    ref, st, r = renderer.render_scene(scene)
+    r.close()
+    H, W = scene["height"], scene["width"]
+    out = torch.zeros(H * W, dtype=torch.int32, device="cuda")
+    bad = dict(scene)
+    d = dict(scene["draws"][0])
+    idx = np.array(d["idx"], np.uint32).copy()
+    idx.reshape(-1)[4] = 0xFFFFFFFF
+    d["idx"] = idx
+    bad["draws"] = [d]
+    assert _noalloc(torch, bad, out) == _lib.INVALID_ARG
+    assert _noalloc(torch, scene, out) == _lib.OK
+    assert (out.cpu().numpy().view(np.uint32).reshape(H, W) == ref).all()
