@@ -132,6 +132,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                 tb += m->ntris;
             }
             F.ntris = tb;
+            if (tb >= kMaxFrameTris) return RAST_INVALID_ARG;  // bin entries hold 28-bit triangle ids
             F.nchunks = row;
             const uint64_t want = std::max<uint64_t>(J.bin_hint, 4ull * tb + F.ntiles + 1024ull);
             F.bin_base = bin_tot;

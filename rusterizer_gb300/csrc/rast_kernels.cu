@@ -71,11 +71,36 @@ __device__ __forceinline__ void unpack_rect(unsigned long long r, uint32_t& x0, 
     x1 = (uint32_t)((r >> 32) & 0xFFFFu);
     y1 = (uint32_t)((r >> 48) & 0xFFFFu);
 }
-__device__ __forceinline__ uint32_t rect_tiles(unsigned long long r) {
+// Tile rectangle (inclusive) of a pixel box (inclusive) for tiles of edge ts.
+__device__ __forceinline__ void tile_rect(unsigned long long r, uint32_t ts, uint32_t& x0, uint32_t& y0,
+                                          uint32_t& x1, uint32_t& y1) {
+    unpack_rect(r, x0, y0, x1, y1);
+    x0 /= ts;
+    y0 /= ts;
+    x1 /= ts;
+    y1 /= ts;
+}
+__device__ __forceinline__ uint32_t rect_tiles(unsigned long long r, uint32_t ts) {
     if (r == kRectEmpty) return 0;
     uint32_t x0, y0, x1, y1;
-    unpack_rect(r, x0, y0, x1, y1);
+    tile_rect(r, ts, x0, y0, x1, y1);
     return (x1 - x0 + 1) * (y1 - y0 + 1);
+}
+// Bin entry of a triangle for tile (tx, ty): triangle << 4 | the raster quadrants of the tile
+// that the triangle's pixel box r touches (bit sy * nsx + sx; a single bit when nsx == 1).
+__device__ __forceinline__ uint32_t bin_entry(uint32_t tri, unsigned long long r, uint32_t tx, uint32_t ty,
+                                              uint32_t ts) {
+    const uint32_t rs = (uint32_t)raster_edge((int)ts);
+    if (rs == ts) return (tri << 4) | 1u;
+    uint32_t px0, py0, px1, py1;
+    unpack_rect(r, px0, py0, px1, py1);
+    const uint32_t ox = tx * ts, oy = ty * ts;
+    const uint32_t sx0 = (max(px0, ox) - ox) / rs, sx1 = (min(px1, ox + ts - 1) - ox) / rs;
+    const uint32_t sy0 = (max(py0, oy) - oy) / rs, sy1 = (min(py1, oy + ts - 1) - oy) / rs;
+    uint32_t m = 0;
+    for (uint32_t sy = sy0; sy <= sy1; ++sy)
+        for (uint32_t sx = sx0; sx <= sx1; ++sx) m |= 1u << (sy * (ts / rs) + sx);
+    return (tri << 4) | m;
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -138,7 +163,7 @@ __global__ void __launch_bounds__(256) k_vertex(const DrawDev* __restrict__ draw
 // ===================================================================== triangle classify
 
 // try_clip + divide + viewport + bounding box for one triangle (src/rasterizer/mod.rs:425-441).
-// Returns its tile rectangle (kRectEmpty when nothing can be covered) and, for a clipped
+// Returns its pixel box (kRectEmpty when nothing can be covered) and, for a clipped
 // triangle, the offset of its polygon in the clip store.
 __device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t tri,
                                   const Scratch& s, unsigned long long& rect, uint32_t& aux) {
@@ -219,8 +244,7 @@ __device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t 
         aux = (uint32_t)off;
         if (bx0 >= bx1 || by0 >= by1) return;
     }
-    const uint32_t ts = (uint32_t)f.ts;
-    rect = pack_rect(bx0 / ts, by0 / ts, (bx1 - 1) / ts, (by1 - 1) / ts);
+    rect = pack_rect(bx0, by0, bx1 - 1, by1 - 1);
 }
 
 // ===================================================================== binning: count
@@ -246,7 +270,7 @@ __global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ 
         s.tri_aux[g] = aux;
         if (rect != kRectEmpty) {
             uint32_t x0, y0, x1, y1;
-            unpack_rect(rect, x0, y0, x1, y1);
+            tile_rect(rect, (uint32_t)f.ts, x0, y0, x1, y1);
             for (uint32_t y = y0; y <= y1; ++y)
                 for (uint32_t x = x0; x <= x1; ++x) atomicAdd(&hist[y * tx + x], 1u);
         }
@@ -356,7 +380,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
     const FrameDev& f = frames[d.frame];
-    const uint32_t nt = f.ntiles, tx = f.tiles_x;
+    const uint32_t nt = f.ntiles, tx = f.tiles_x, ts = (uint32_t)f.ts;
     const uint32_t* crow = s.counts + f.count_base + (unsigned long long)ch.row * nt;
     for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x)
         run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
@@ -376,7 +400,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         const uint32_t i = base + threadIdx.x;
         const bool live = i < ch.tri_count;
         const unsigned long long rect = live ? s.tri_rect[gbase + i] : kRectEmpty;
-        const uint32_t n = rect_tiles(rect);
+        const uint32_t n = rect_tiles(rect, ts);
         uint32_t total;
         const uint32_t excl = block_excl_scan(n, tmp, total);
         if (threadIdx.x == 0) {
@@ -392,12 +416,13 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             // a single large triangle: its tiles are distinct, each takes the next position
             const uint32_t g0 = d.tbase + ch.tri_begin + base;
             uint32_t x0, y0, x1, y1;
-            unpack_rect(r0, x0, y0, x1, y1);
+            tile_rect(r0, ts, x0, y0, x1, y1);
             const uint32_t w = x1 - x0 + 1;
             for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
-                const uint32_t t = (y0 + k / w) * tx + x0 + k % w;
+                const uint32_t ttx = x0 + k % w, tty = y0 + k / w;
+                const uint32_t t = tty * tx + ttx;
                 const uint32_t pos = run_off[t];
-                if (pos < cap) bins[pos] = g0;
+                if (pos < cap) bins[pos] = bin_entry(g0, r0, ttx, tty, ts);
                 run_off[t] = pos + 1;
             }
             __syncthreads();
@@ -407,7 +432,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         const bool part = live && (excl + n <= (uint32_t)kPairsPerBatch);
         const uint32_t take = __syncthreads_count(part);
         uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-        if (part && n) unpack_rect(rect, x0, y0, x1, y1);
+        if (part && n) tile_rect(rect, ts, x0, y0, x1, y1);
         if (part && n) {
             for (uint32_t y = y0; y <= y1; ++y)
                 for (uint32_t x = x0; x <= x1; ++x) {
@@ -435,7 +460,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                     uint32_t before = __popc(hmask[h][warp] & lanemask_lt());
                     for (uint32_t w2 = 0; w2 < warp; ++w2) before += __popc(hmask[h][w2]);
                     const uint32_t pos = run_off[t] + before;
-                    if (pos < cap) bins[pos] = frame_tri;
+                    if (pos < cap) bins[pos] = bin_entry(frame_tri, rect, x, y, ts);
                 }
         }
         __syncthreads();
@@ -463,13 +488,15 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 constexpr int kRasterThreads = 256;
 constexpr int kRasterWarps = kRasterThreads / 32;
 
+// A raster CTA owns one TS x TS tile: a whole bin (bin edge == TS) or one quadrant of a bin
+// twice as wide. Bin entries carry, in their low 4 bits, the quadrants the triangle's pixel box
+// touches, so a quadrant CTA skips the other entries without loading them.
 template <int S, int TS>
 struct RasterCfg {
     static constexpr int NPIX = TS * TS;
-    static constexpr int RW = TS / kRasterWarps;  // rows per warp: w, w + 8, w + 16, ...
     static constexpr int IC = kRasterThreads;  // items (triangles after clipping) per batch
     static constexpr int QC = 64;              // per-warp fragment ring
-    static_assert(TS % kRasterWarps == 0, "tile rows must split evenly over the warps");
+    static_assert(TS <= 32, "one lane per tile row or column in the work split");
 };
 
 template <int S, int TS>
@@ -483,7 +510,7 @@ struct RasterSmem {
     uint32_t irect[C::IC];  // tile-local pixel box: x0 | y0 << 8 | x1 << 16 | y1 << 24
     uint32_t itri[C::IC];
     uint32_t imeta[C::IC];  // draw << 8 | sub-triangle
-    uint32_t member[kRasterWarps][C::IC / 32];  // bit: item overlaps one of the warp's rows
+    uint32_t member[kRasterWarps][C::IC / 32];  // bit: item overlaps the warp's rows/columns
     uint16_t wlist[kRasterWarps][C::IC];         // the warp's items, in submission order
     // per-warp rings of covered fragments, in submission order
     float qz[kRasterWarps][S][C::QC];
@@ -491,8 +518,10 @@ struct RasterSmem {
     uint16_t qpix[kRasterWarps][C::QC];
     uint8_t qcov[kRasterWarps][C::QC];
     float inv255[256];
+    int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
+    uint32_t own[kRasterWarps + 1];  // warp w owns tile rows (or columns) [own[w], own[w+1])
     uint32_t tmp[40];
-    uint32_t misc[8];
+    uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split axis
 };
 
 template <int S, int TS>
@@ -528,6 +557,138 @@ __device__ __forceinline__ void item_normal(const RasterSmem<S, TS>& sm, uint32_
     const float vy = sm.ipy[n][it] - sm.ipy[k][it];
     nx = -vy;
     ny = vx;
+}
+
+// Stages the items of one bin entry (one triangle, or the fan of its clipped polygon) at
+// positions first.. of the batch: screen points, depths, w, attributes, 1 / 2x area and the
+// tile-local pixel box, and adds the box to the batch's row and column work.
+template <int S, int TS>
+__device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDev& f,
+                                            const DrawDev* __restrict__ draws, const Scratch& s,
+                                            uint32_t g, uint32_t aux, uint32_t nitems, uint32_t first,
+                                            uint32_t X0, uint32_t Y0) {
+    const uint32_t di = find_draw(draws, f, g);
+    const DrawDev& d = draws[di];
+    const int fs = d.fs;
+    for (uint32_t k = 0; k < nitems; ++k) {
+        const uint32_t it = first + k;
+        float4 sv[3];
+        float at[3][6];
+        if (aux == kNone) {
+            const uint32_t tri = g - d.tbase;
+            const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
+                                    __ldg(d.idx + 3ull * tri + 2)};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                sv[q] = s.vscr[d.vbase + ii[q]];
+                if (fs == 1) {
+                    if (d.rgba) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
+                    }
+                } else if (fs == 0) {
+                    at[q][4] = __ldg(d.uv + 2ull * ii[q]);
+                    at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
+                }
+            }
+        } else {
+            const float* st = s.clip_store + aux + 1;
+            const uint32_t vi[3] = {0u, k + 1, k + 2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float* o = st + 10 * vi[q];
+                sv[q] = make_float4(o[0], o[1], o[2], o[3]);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) at[q][c] = o[4 + c];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            sm.ipx[q][it] = sv[q].x;
+            sm.ipy[q][it] = sv[q].y;
+            sm.iz[q][it] = sv[q].z;
+            sm.iw[q][it] = sv[q].w;
+            if (fs == 0) {
+                sm.iat[2 * q][it] = at[q][4];
+                sm.iat[2 * q + 1][it] = at[q][5];
+            } else if (fs == 1) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) sm.iat[4 * q + c][it] = at[q][c];
+            }
+        }
+        // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
+        sm.iinv[it] = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
+        uint32_t bx0, bx1, by0, by1;
+        pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
+        const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
+        const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
+        const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1;
+        uint32_t r = 0;
+        if (nonempty) {
+            const uint32_t lx0 = cx0 - X0, ly0 = cy0 - Y0, lx1 = cx1 - X0, ly1 = cy1 - Y0;
+            r = lx0 | (ly0 << 8) | (lx1 << 16) | (ly1 << 24);
+            const int cw = (int)(lx1 - lx0), chh = (int)(ly1 - ly0);
+            atomicAdd(&sm.rowd[ly0], cw);
+            atomicAdd(&sm.rowd[ly1], -cw);
+            atomicAdd(&sm.cold[lx0], chh);
+            atomicAdd(&sm.cold[lx1], -chh);
+        }
+        sm.irect[it] = r;
+        sm.itri[it] = g;
+        sm.imeta[it] = (di << 8) | k;
+    }
+}
+
+// Splits the tile's rows, or its columns, into kRasterWarps contiguous ranges of about equal
+// candidate-pixel work and keeps the axis whose heaviest range is lighter (rows suit scattered
+// triangles, columns suit runs of small triangles along a screen row). Each warp then owns the
+// pixels of its range for the batch, which keeps every pixel's fragments in one warp and in
+// submission order. Called by one warp.
+template <int TS>
+__device__ __forceinline__ void split_work(const int* rowd, const int* cold, uint32_t* own,
+                                           uint32_t* axis_out) {
+    const uint32_t lane = lane_id();
+    uint32_t best = 0xFFFFFFFFu, best_axis = 0, best_part = 0;
+    for (uint32_t axis = 0; axis < 2; ++axis) {
+        const int* dd = axis == 0 ? rowd : cold;
+        int lw = lane < (uint32_t)TS ? dd[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, lw, o);
+            if (lane >= (uint32_t)o) lw += y;
+        }
+        const uint32_t wl = lane < (uint32_t)TS ? (uint32_t)lw : 0u;  // work of line `lane`
+        uint32_t incl = wl;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const uint32_t excl = incl - wl;
+        uint32_t part;
+        if (lane >= (uint32_t)TS) part = kRasterWarps;
+        else if (total == 0) part = lane * kRasterWarps / TS;
+        else part = min((uint32_t)(kRasterWarps - 1), ((2u * excl + wl) * kRasterWarps) / (2u * total));
+        uint32_t mx = 0;
+#pragma unroll
+        for (int k = 0; k < kRasterWarps; ++k)
+            mx = max(mx, __reduce_add_sync(0xFFFFFFFFu, part == (uint32_t)k ? wl : 0u));
+        if (mx < best) {
+            best = mx;
+            best_axis = axis;
+            best_part = part;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k <= kRasterWarps; ++k) {
+        const uint32_t b = __popc(__ballot_sync(0xFFFFFFFFu, best_part < (uint32_t)k));
+        if (lane == 0) own[k] = b;
+    }
+    if (lane == 0) *axis_out = best_axis;
 }
 
 // Depth test, shading and colour write of up to 32 queued fragments of one warp (lane = one
@@ -632,11 +793,36 @@ __device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, 
     }
 }
 
+// Writes the clear colour (and, when captured, clear samples) over one tile of a frame.
+__device__ __forceinline__ void clear_tile_warp(const FrameDev& f, uint32_t x0, uint32_t y0,
+                                                uint32_t edge, int S) {
+    const uint32_t lane = lane_id();
+    for (uint32_t i = lane; i < edge * edge; i += 32) {
+        const uint32_t x = x0 + i % edge, y = y0 + i / edge;
+        if (x >= f.width || y >= f.height) continue;
+        const unsigned long long o = (unsigned long long)y * f.width + x;
+        f.out[o] = kClearColor;
+        if (f.dbg_depth) {
+            for (int q = 0; q < S; ++q) {
+                f.dbg_depth[o * S + q] = f.clear_depth;
+                f.dbg_color[o * S + q] = kClearColor;
+            }
+        }
+    }
+}
+
+// Persistent raster kernel. Units are (bin with entries, quadrant) pairs taken heaviest bin
+// first from queue[0]; per unit the CTA replays the bin in submission order in batches of up
+// to IC items: stage the items (A), split the tile's rows or columns over the warps by work
+// (B), then each warp walks the candidate pixels of its items inside its range — coverage
+// (EdgeFunctions::eval, mod.rs:134-146) and sample depths (RasterizerTriangle::fragment,
+// mod.rs:225-253) — and depth-tests, shades and writes the covered fragments in order (C).
+// Bins without entries are then cleared by single warps from queue[1].
 template <int S, int TS>
 __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __restrict__ frames,
                                                            int nframes,
                                                            const uint32_t* __restrict__ order,
-                                                           uint32_t ntotal,
+                                                           uint32_t ntotal, uint32_t nsx,
                                                            unsigned int* __restrict__ queue,
                                                            const DrawDev* __restrict__ draws,
                                                            Scratch s) {
@@ -647,123 +833,75 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
     sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
     uint32_t shaded = 0, fsinv = 0, oobc = 0;
     const uint32_t nbusy = *(volatile unsigned int*)&queue[2];  // written by k_tile_order
+    const uint32_t nsub = nsx * nsx;
 
-    // persistent loop over the tiles that have entries, heaviest first
     for (;;) {
     if (threadIdx.x == 0) sm.misc[0] = atomicAdd(&queue[0], 1u);
     __syncthreads();
     const uint32_t qi = sm.misc[0];
     __syncthreads();
-    if (qi >= nbusy) break;
-    const uint32_t gt = order[qi];
+    if (qi >= nbusy * nsub) break;
+    const uint32_t gt = order[qi / nsub], sub = qi % nsub;
     const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
     const uint32_t lt = gt - f.tile_begin;
-    const uint32_t X0 = (lt % f.tiles_x) * TS, Y0 = (lt / f.tiles_x) * TS;
+    const uint32_t X0 = (lt % f.tiles_x) * (uint32_t)f.ts + (sub % nsx) * TS;
+    const uint32_t Y0 = (lt / f.tiles_x) * (uint32_t)f.ts + (sub / nsx) * TS;
     const uint32_t W = f.width, H = f.height;
     for (uint32_t i = threadIdx.x; i < (uint32_t)(C::NPIX * S); i += blockDim.x) {
         sm.zb[i] = f.clear_depth;
         sm.cb[i] = kClearColor;
     }
-    __syncthreads();
     const uint32_t nent = s.tile_count[gt];
     const uint32_t* bins = s.bins + f.bin_base + s.tile_start[gt];
+    const uint32_t mybit = 1u << sub;
 
-    for (uint32_t e0 = 0; e0 < nent;) {
-        // ---- A. entries -> items (sub-triangles after clipping, in fan order), one thread per entry
-        const uint32_t e = e0 + threadIdx.x;
-        uint32_t g = 0, aux = kNone, nitems = 0;
-        if (e < nent) {
-            g = bins[e];
-            aux = s.tri_aux[f.rect_base + g];
-            nitems = (aux == kNone) ? 1u : (uint32_t)__float_as_int(s.clip_store[aux]) - 2u;
+    uint32_t pos = 0;  // next entry of the bin
+    while (pos < nent) {
+        // ---- A. fill a batch with the items of the next entries that touch this tile
+        if (threadIdx.x <= (uint32_t)TS) {
+            sm.rowd[threadIdx.x] = 0;
+            sm.cold[threadIdx.x] = 0;
         }
-        uint32_t itot;
-        const uint32_t iex = block_excl_scan(nitems, sm.tmp, itot);
-        const bool part = (e < nent) && (iex + nitems <= (uint32_t)C::IC);
-        const uint32_t take = __syncthreads_count(part);
-        if (part && threadIdx.x == take - 1) sm.misc[1] = iex + nitems;
-        if (part) {
-            const uint32_t di = find_draw(draws, f, g);
-            const DrawDev& d = draws[di];
-            const int fs = d.fs;
-            for (uint32_t k = 0; k < nitems; ++k) {
-                const uint32_t it = iex + k;
-                float4 sv[3];
-                float at[3][6];
-                if (aux == kNone) {
-                    const uint32_t tri = g - d.tbase;
-                    const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
-                                            __ldg(d.idx + 3ull * tri + 2)};
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        sv[q] = s.vscr[d.vbase + ii[q]];
-                        if (fs == 1) {
-                            if (d.rgba) {
-#pragma unroll
-                                for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
-                            } else {
-#pragma unroll
-                                for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
-                            }
-                        } else if (fs == 0) {
-                            at[q][4] = __ldg(d.uv + 2ull * ii[q]);
-                            at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
-                        }
-                    }
-                } else {
-                    const float* st = s.clip_store + aux + 1;
-                    const uint32_t vi[3] = {0u, k + 1, k + 2};
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        const float* o = st + 10 * vi[q];
-                        sv[q] = make_float4(o[0], o[1], o[2], o[3]);
-#pragma unroll
-                        for (int c = 0; c < 6; ++c) at[q][c] = o[4 + c];
-                    }
+        uint32_t nit = 0;
+        while (pos < nent) {
+            const uint32_t e = pos + threadIdx.x;
+            uint32_t g = 0, aux = kNone, nitems = 0;
+            if (e < nent) {
+                const uint32_t ent = bins[e];
+                if (ent & mybit) {
+                    g = ent >> 4;
+                    aux = s.tri_aux[f.rect_base + g];
+                    nitems = (aux == kNone) ? 1u : (uint32_t)__float_as_int(s.clip_store[aux]) - 2u;
                 }
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    sm.ipx[q][it] = sv[q].x;
-                    sm.ipy[q][it] = sv[q].y;
-                    sm.iz[q][it] = sv[q].z;
-                    sm.iw[q][it] = sv[q].w;
-                    if (fs == 0) {
-                        sm.iat[2 * q][it] = at[q][4];
-                        sm.iat[2 * q + 1][it] = at[q][5];
-                    } else if (fs == 1) {
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) sm.iat[4 * q + c][it] = at[q][c];
-                    }
-                }
-                // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
-                sm.iinv[it] = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
-                uint32_t bx0, bx1, by0, by1;
-                pixel_bbox(sv, W, H, bx0, bx1, by0, by1);
-                const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
-                const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
-                const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1;
-                sm.irect[it] = nonempty ? ((cx0 - X0) | ((cy0 - Y0) << 8) | ((cx1 - X0) << 16) |
-                                           ((cy1 - Y0) << 24))
-                                        : 0u;
-                sm.itri[it] = g;
-                sm.imeta[it] = (di << 8) | k;
             }
+            if (threadIdx.x == 0) sm.misc[1] = nit;
+            uint32_t itot;
+            const uint32_t iex = block_excl_scan(nitems, sm.tmp, itot);
+            const bool part = (e < nent) && (nit + iex + nitems <= (uint32_t)C::IC);
+            const uint32_t take = __syncthreads_count(part);
+            if (part && threadIdx.x == take - 1) sm.misc[1] = nit + iex + nitems;
+            if (part && nitems) stage_entry<S, TS>(sm, f, draws, s, g, aux, nitems, nit + iex, X0, Y0);
+            __syncthreads();
+            nit = sm.misc[1];
+            const uint32_t window = min(nent - pos, (uint32_t)kRasterThreads);
+            pos += take;
+            if (take < window) break;  // the batch is full
         }
+        // ---- B. split rows or columns over the warps; which warps each item reaches
+        if (warp == 0) split_work<TS>(sm.rowd, sm.cold, sm.own, &sm.misc[5]);
         __syncthreads();
-        const uint32_t nit = sm.misc[1];
-        // ---- B. which warps own a row of each item's box (warp w owns rows w, w+8, ...)
+        const uint32_t axis = sm.misc[5];
         {
             const uint32_t t = threadIdx.x;
             uint32_t wm = 0;
             if (t < nit) {
                 const uint32_t r = sm.irect[t];
-                const uint32_t ly0 = (r >> 8) & 0xFFu, ly1 = r >> 24;
-                if (ly1 > ly0) {
-                    const uint32_t nrow = ly1 - ly0;
-                    wm = nrow >= (uint32_t)kRasterWarps
-                             ? (1u << kRasterWarps) - 1u
-                             : (((1u << nrow) - 1u) << (ly0 % kRasterWarps));
-                    wm = (wm | (wm >> kRasterWarps)) & ((1u << kRasterWarps) - 1u);
+                const uint32_t a0 = axis ? (r & 0xFFu) : ((r >> 8) & 0xFFu);
+                const uint32_t a1 = axis ? ((r >> 16) & 0xFFu) : (r >> 24);
+                if (a1 > a0) {
+#pragma unroll
+                    for (int w = 0; w < kRasterWarps; ++w)
+                        if (a0 < sm.own[w + 1] && a1 > sm.own[w]) wm |= 1u << w;
                 }
             }
 #pragma unroll
@@ -773,9 +911,9 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             }
         }
         __syncthreads();
-        // ---- C. per warp, in submission order: candidate pixels of its band, coverage
-        // (EdgeFunctions::eval, mod.rs:134-146), sample depths (RasterizerTriangle::fragment,
-        // mod.rs:225-253), then ordered depth test and shading of the covered fragments
+        // ---- C. per warp, in submission order: candidate pixels of its range, coverage and
+        // sample depths, then ordered depth test and shading of the covered fragments
+        const uint32_t olo = sm.own[warp], ohi = sm.own[warp + 1];
         uint32_t nmine = 0;
 #pragma unroll
         for (int src = 0; src < C::IC / 32; ++src) {
@@ -791,14 +929,18 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             uint32_t cx0 = 0, cw = 1, cy0 = 0, c = 0;
             if (act) {
                 const uint32_t r = sm.irect[it_l];
-                const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
-                // first row of the box owned by this warp, then every kRasterWarps-th row
-                const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
-                const uint32_t nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
+                uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
+                if (axis) {
+                    lx0 = max(lx0, olo);
+                    lx1 = min(lx1, ohi);
+                } else {
+                    ly0 = max(ly0, olo);
+                    ly1 = min(ly1, ohi);
+                }
                 cx0 = lx0;
                 cw = lx1 - lx0;
-                cy0 = first;
-                c = cw * nrows;
+                cy0 = ly0;
+                c = cw * (ly1 - ly0);
             }
             uint32_t incl = c;
 #pragma unroll
@@ -828,7 +970,7 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
                 for (int k = 0; k < S; ++k) z[k] = 0.0f;
                 if (p < total) {
                     const uint32_t rr = p - exc;
-                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + kRasterWarps * (rr / sw);
+                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + rr / sw;
                     pix = ly * TS + lx;
                     const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
                     float n0x, n0y, n1x, n1y, n2x, n2y;
@@ -876,11 +1018,11 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             }
         }
         if (tail != head) warp_process<S, TS>(sm, warp, head, tail - head, draws, s, X0, Y0, shaded, fsinv, oobc);
-        e0 += take;
         __syncthreads();
     }
 
     // ---- resolve (resolve_and_clear + box_filter_color, mod.rs:478-518, buffers.rs:111-125)
+    __syncthreads();
     for (uint32_t p = threadIdx.x; p < (uint32_t)C::NPIX; p += blockDim.x) {
         const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
         if (x >= W || y >= H) continue;
@@ -894,10 +1036,9 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             }
         }
     }
-    }  // tiles with entries
+    }  // units with entries
 
-    // ---- tiles without entries: warps take whole tiles independently and write the resolve
-    // of clear samples (the clear colour)
+    // ---- bins without entries: warps take whole bins and write the clear colour
     for (;;) {
         uint32_t qi = 0;
         if (lane == 0) qi = atomicAdd(&queue[1], 1u);
@@ -906,20 +1047,8 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
         const uint32_t gt = order[qi];
         const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
         const uint32_t lt = gt - f.tile_begin;
-        const uint32_t x0 = (lt % f.tiles_x) * TS, y0 = (lt / f.tiles_x) * TS;
-        for (uint32_t i = lane; i < (uint32_t)C::NPIX; i += 32) {
-            const uint32_t x = x0 + i % TS, y = y0 + i / TS;
-            if (x >= f.width || y >= f.height) continue;
-            const unsigned long long o = (unsigned long long)y * f.width + x;
-            f.out[o] = kClearColor;
-            if (f.dbg_depth) {
-#pragma unroll
-                for (int q = 0; q < S; ++q) {
-                    f.dbg_depth[o * S + q] = f.clear_depth;
-                    f.dbg_color[o * S + q] = kClearColor;
-                }
-            }
-        }
+        const uint32_t edge = (uint32_t)f.ts;
+        clear_tile_warp(f, (lt % f.tiles_x) * edge, (lt / f.tiles_x) * edge, edge, S);
     }
     // per-block statistics
     __syncthreads();
@@ -980,7 +1109,7 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
 // ===================================================================== launchers
 
 template <int S, int TS>
-static cudaError_t launch_raster_t(const LaunchArgs& a) {
+static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
     static int grid_cap = 0;
     if (!grid_cap) {
@@ -997,10 +1126,11 @@ static cudaError_t launch_raster_t(const LaunchArgs& a) {
     if (a.raster_blocks == 0) return cudaSuccess;
     k_tile_order<<<1, 1024, 0, a.stream>>>(a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
                                            a.scratch.tile_order, a.raster_queue, a.scratch.status);
-    const unsigned grid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
+    const unsigned long long units = (unsigned long long)a.raster_blocks * nsx * nsx;
+    const unsigned grid = units < (unsigned long long)grid_cap ? (unsigned)units : (unsigned)grid_cap;
     k_raster<S, TS><<<grid, kRasterThreads, bytes, a.stream>>>(
         a.raster_frames, a.raster_nframes, a.scratch.tile_order + a.raster_tile_offset, a.raster_blocks,
-        a.raster_queue, a.draws, a.scratch);
+        nsx, a.raster_queue, a.draws, a.scratch);
     return cudaGetLastError();
 }
 
@@ -1044,28 +1174,20 @@ cudaError_t launch_bin_scatter(const LaunchArgs& a) {
 }
 
 cudaError_t launch_raster(const LaunchArgs& a, int msaa, int ts) {
-    if (msaa == 4) {
-        if (ts == 8) return launch_raster_t<4, 8>(a);
-        if (ts == 16) return launch_raster_t<4, 16>(a);
-        if (ts == 32) return launch_raster_t<4, 32>(a);
-    } else if (msaa == 1) {
-        if (ts == 8) return launch_raster_t<1, 8>(a);
-        if (ts == 16) return launch_raster_t<1, 16>(a);
-        if (ts == 32) return launch_raster_t<1, 32>(a);
-    }
+    // bins of edge ts are rastered as tiles of edge raster_edge(ts) (quadrants of 32-pixel bins)
+    if (ts != 8 && ts != 16 && ts != 32) return cudaErrorInvalidValue;
+    const int rs = raster_edge(ts);
+    const uint32_t nsx = (uint32_t)(ts / rs);
+    if (msaa == 4) return rs == 8 ? launch_raster_t<4, 8>(a, nsx) : launch_raster_t<4, 16>(a, nsx);
+    if (msaa == 1) return rs == 8 ? launch_raster_t<1, 8>(a, nsx) : launch_raster_t<1, 16>(a, nsx);
     return cudaErrorInvalidValue;
 }
 
 size_t raster_smem(int msaa, int ts) {
-    if (msaa == 4) {
-        if (ts == 8) return raster_smem_bytes<4, 8>();
-        if (ts == 16) return raster_smem_bytes<4, 16>();
-        if (ts == 32) return raster_smem_bytes<4, 32>();
-    } else if (msaa == 1) {
-        if (ts == 8) return raster_smem_bytes<1, 8>();
-        if (ts == 16) return raster_smem_bytes<1, 16>();
-        if (ts == 32) return raster_smem_bytes<1, 32>();
-    }
+    if (ts != 8 && ts != 16 && ts != 32) return 0;
+    const int rs = raster_edge(ts);
+    if (msaa == 4) return rs == 8 ? raster_smem_bytes<4, 8>() : raster_smem_bytes<4, 16>();
+    if (msaa == 1) return rs == 8 ? raster_smem_bytes<1, 8>() : raster_smem_bytes<1, 16>();
     return 0;
 }
 

@@ -7,12 +7,13 @@
 //   vclip[v]  float4  clip-space position of vertex v (MVP * (x,y,z,1))
 //   vscr[v]   float4  (screen x, screen y, screen z, w) after divide + viewport
 //   vcode[v]  u16     clip predicates (rast_device.cuh clip_code)
-//   tri_rect[t] u64   tile rectangle of triangle t (x0,y0,x1,y1 inclusive, 16 bits each),
+//   tri_rect[t] u64   pixel box of triangle t (x0,y0,x1,y1 inclusive, 16 bits each),
 //                     kRectEmpty when culled
 //   tri_aux[t]  u32   offset of the clipped polygon in clip_store, kNone when unclipped
 //   counts[frame][chunk][tile] u32  per-chunk tile histograms, then exclusive prefixes
 //   tile_start / tile_count [tile]  each tile's bin range
-//   bins[]    u32     per-tile triangle lists in submission order
+//   bins[]    u32     per-tile lists in submission order: triangle << 4 | mask of the
+//                     raster quadrants of the bin that its pixel box touches
 // Per-sample colour and depth never touch HBM: they live in shared memory of the tile CTA.
 #pragma once
 
@@ -26,6 +27,14 @@ constexpr int kMaxPoly = 32;                   // clip polygon capacity (a conve
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kRectEmpty = ~0ull;
 constexpr int kMaxTilesPerFrame = 16384;       // per-frame tile count limit (smem histograms)
+constexpr uint32_t kMaxFrameTris = 1u << 28;     // bin entries hold triangle << 4 | quadrant mask
+
+// Edge of the raster tile that one CTA owns for bins of edge ts: 32-pixel bins are rastered as
+// four 16-pixel quadrants (more, smaller units balance the persistent raster kernel better).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr int raster_edge(int ts) { return ts > 16 ? 16 : ts; }
 
 enum StatusBits : uint32_t {
     ST_TEXTURE_OOB = 1u << 0,

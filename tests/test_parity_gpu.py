@@ -158,12 +158,12 @@ def test_out_of_range_index_detected_on_device():
     blk.view, blk.projection, blk.world = s["view"], s["proj"], d["world"]
     bad = np.array(d["idx"], np.uint32).copy()
     bad.reshape(-1)[5] = len(d["pos"])  # one past the end
-    r.update(d, d["pos"], d["uv"], bad)
+    r.update(d, d["pos"], d["uv"], bad, d.get("rgba"))
     r.render(d, renderer.VS_MVP, d.get("fs", 0))
     with pytest.raises(_lib.RastError) as e:
         r.framebuffer()
     assert e.value.status == _lib.INVALID_ARG
-    r.update(d, d["pos"], d["uv"], d["idx"])
+    r.update(d, d["pos"], d["uv"], d["idx"], d.get("rgba"))
     r.render(d, renderer.VS_MVP, d.get("fs", 0))
     img = r.framebuffer()
     ref, *_ = oracle.render_scene(s)
