@@ -76,7 +76,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         draws.clear();
         chunks.clear();
         vblocks.clear();
-        uint64_t vtot = 0, ttot = 0, count_tot = 0, bin_tot = 0, clip_est = 0;
+        uint64_t vtot = 0, ttot = 0, count_tot = 0, bin_tot = 0, qbin_tot = 0, clip_est = 0;
         uint32_t tile_tot = 0, group_tot = 0, max_tiles = 1;
         for (size_t oi = 0; oi < order.size(); ++oi) {
             FrameJob& J = jobs[order[oi]];
@@ -132,12 +132,14 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                 tb += m->ntris;
             }
             F.ntris = tb;
-            if (tb >= kMaxFrameTris) return RAST_INVALID_ARG;  // bin entries hold 28-bit triangle ids
+            if (tb >= kMaxFrameTris) return RAST_INVALID_ARG;  // bin entries hold 27-bit triangle ids
             F.nchunks = row;
             const uint64_t want = std::max<uint64_t>(J.bin_hint, 4ull * tb + F.ntiles + 1024ull);
             F.bin_base = bin_tot;
             F.bin_cap = want;
             bin_tot += want;
+            F.qbin_base = qbin_tot;
+            if (raster_edge(J.ts) < J.ts) qbin_tot += 4ull * want;
             clip_est += 32ull * tb + 4096ull;
             count_tot += (uint64_t)F.nchunks * F.ntiles;
             ttot += tb;
@@ -153,7 +155,8 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                   E.tri_rect.reserve(ttot) && E.tri_aux.reserve(ttot) &&
                   E.counts.reserve(count_tot) && E.tile_start.reserve(tile_tot) &&
                   E.tile_count.reserve(tile_tot) && E.tile_order.reserve(tile_tot) &&
-                  E.bins.reserve(bin_tot) &&
+                  E.bins.reserve(bin_tot) && E.qbins.reserve(qbin_tot) &&
+                  E.qcount.reserve(qbin_tot ? 4ull * tile_tot : 0ull) &&
                   E.clip_store.reserve(std::max<uint64_t>(clip_est, E.clip_hint)) &&
                   E.frame_need.reserve(frames.size());
         if (!ok) return RAST_OOM;
@@ -212,6 +215,8 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         S.tile_count = E.tile_count.p;
         S.tile_order = E.tile_order.p;
         S.bins = E.bins.p;
+        S.qbins = E.qbins.p;
+        S.qcount = E.qcount.p;
         S.clip_store = E.clip_store.p;
         S.clip_cap = E.clip_store.cap;
         S.clip_used = &E.d_state->clip_used;

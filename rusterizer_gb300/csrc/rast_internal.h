@@ -182,7 +182,7 @@ struct Engine {
     DevBuf<float4> vclip, vscr;
     DevBuf<uint16_t> vcode;
     DevBuf<unsigned long long> tri_rect;
-    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, tile_order, bins;
+    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, tile_order, bins, qbins, qcount;
     DevBuf<float> clip_store;
     DevBuf<unsigned long long> frame_need;
     DevBuf<uint32_t> log;

@@ -86,12 +86,14 @@ __device__ __forceinline__ uint32_t rect_tiles(unsigned long long r, uint32_t ts
     tile_rect(r, ts, x0, y0, x1, y1);
     return (x1 - x0 + 1) * (y1 - y0 + 1);
 }
-// Bin entry of a triangle for tile (tx, ty): triangle << 4 | the raster quadrants of the tile
-// that the triangle's pixel box r touches (bit sy * nsx + sx; a single bit when nsx == 1).
-__device__ __forceinline__ uint32_t bin_entry(uint32_t tri, unsigned long long r, uint32_t tx, uint32_t ty,
-                                              uint32_t ts) {
+// Bin entry of a triangle for tile (tx, ty): triangle << 5 | clipped << 4 | the raster
+// quadrants of the tile that the triangle's pixel box r touches (bit sy * nsx + sx; a single
+// bit when nsx == 1).
+__device__ __forceinline__ uint32_t bin_entry(uint32_t tri, bool clipped, unsigned long long r, uint32_t tx,
+                                              uint32_t ty, uint32_t ts) {
+    const uint32_t head = (tri << kEntShift) | (clipped ? kEntClipped : 0u);
     const uint32_t rs = (uint32_t)raster_edge((int)ts);
-    if (rs == ts) return (tri << 4) | 1u;
+    if (rs == ts) return head | 1u;
     uint32_t px0, py0, px1, py1;
     unpack_rect(r, px0, py0, px1, py1);
     const uint32_t ox = tx * ts, oy = ty * ts;
@@ -100,7 +102,7 @@ __device__ __forceinline__ uint32_t bin_entry(uint32_t tri, unsigned long long r
     uint32_t m = 0;
     for (uint32_t sy = sy0; sy <= sy1; ++sy)
         for (uint32_t sx = sx0; sx <= sx1; ++sx) m |= 1u << (sy * (ts / rs) + sx);
-    return (tri << 4) | m;
+    return head | m;
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -356,6 +358,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict_
 
 constexpr int kScatterThreads = 256;
 constexpr int kPairsPerBatch = 512;  // (triangle, tile) pairs ranked per batch
+constexpr uint32_t kBigTri = 32;     // triangles over more tiles are binned alone, tile-parallel
 constexpr int kHashSlots = 1024;     // open-addressing table over tile ids, load <= 0.5
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
 
@@ -376,6 +379,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     __shared__ uint32_t nslots;
     __shared__ uint32_t tmp[33];
     __shared__ unsigned long long rect0;
+    __shared__ uint32_t aux0, n0s, big0;
     if (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) return;
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
@@ -400,19 +404,25 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         const uint32_t i = base + threadIdx.x;
         const bool live = i < ch.tri_count;
         const unsigned long long rect = live ? s.tri_rect[gbase + i] : kRectEmpty;
+        const bool clipped = live && s.tri_aux[gbase + i] != kNone;
         const uint32_t n = rect_tiles(rect, ts);
-        uint32_t total;
-        const uint32_t excl = block_excl_scan(n, tmp, total);
         if (threadIdx.x == 0) {
-            tmp[0] = n;
+            big0 = kScatterThreads;
+            n0s = n;
             rect0 = rect;
+            aux0 = clipped;
         }
+        uint32_t total;
+        const uint32_t excl = block_excl_scan(n, tmp, total);  // its barriers order big0
+        if (n > kBigTri) atomicMin(&big0, threadIdx.x);
         __syncthreads();
-        const uint32_t n0 = tmp[0];
+        const uint32_t n0 = n0s;
         const unsigned long long r0 = rect0;
+        const bool c0 = aux0 != 0;
+        const uint32_t firstbig = big0;
         __syncthreads();
         const uint32_t frame_tri = d.tbase + ch.tri_begin + i;  // bin entry: triangle in frame
-        if (n0 > (uint32_t)kPairsPerBatch) {
+        if (firstbig == 0) {
             // a single large triangle: its tiles are distinct, each takes the next position
             const uint32_t g0 = d.tbase + ch.tri_begin + base;
             uint32_t x0, y0, x1, y1;
@@ -422,14 +432,15 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                 const uint32_t ttx = x0 + k % w, tty = y0 + k / w;
                 const uint32_t t = tty * tx + ttx;
                 const uint32_t pos = run_off[t];
-                if (pos < cap) bins[pos] = bin_entry(g0, r0, ttx, tty, ts);
+                if (pos < cap) bins[pos] = bin_entry(g0, c0, r0, ttx, tty, ts);
                 run_off[t] = pos + 1;
             }
             __syncthreads();
             base += 1;
             continue;
         }
-        const bool part = live && (excl + n <= (uint32_t)kPairsPerBatch);
+        // a prefix of small triangles: stop at the first large one and at the pair budget
+        const bool part = live && threadIdx.x < firstbig && (excl + n <= (uint32_t)kPairsPerBatch);
         const uint32_t take = __syncthreads_count(part);
         uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
         if (part && n) tile_rect(rect, ts, x0, y0, x1, y1);
@@ -460,7 +471,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                     uint32_t before = __popc(hmask[h][warp] & lanemask_lt());
                     for (uint32_t w2 = 0; w2 < warp; ++w2) before += __popc(hmask[h][w2]);
                     const uint32_t pos = run_off[t] + before;
-                    if (pos < cap) bins[pos] = bin_entry(frame_tri, rect, x, y, ts);
+                    if (pos < cap) bins[pos] = bin_entry(frame_tri, clipped, rect, x, y, ts);
                 }
         }
         __syncthreads();
@@ -519,9 +530,10 @@ struct RasterSmem {
     uint8_t qcov[kRasterWarps][C::QC];
     float inv255[256];
     int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
-    uint32_t own[kRasterWarps + 1];  // warp w owns tile rows (or columns) [own[w], own[w+1])
+    uint32_t own[kRasterWarps + 1];  // column mode: warp w owns columns [own[w], own[w+1])
     uint32_t tmp[40];
-    uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split axis
+    uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split mode
+
 };
 
 template <int S, int TS>
@@ -642,53 +654,56 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
     }
 }
 
-// Splits the tile's rows, or its columns, into kRasterWarps contiguous ranges of about equal
-// candidate-pixel work and keeps the axis whose heaviest range is lighter (rows suit scattered
-// triangles, columns suit runs of small triangles along a screen row). Each warp then owns the
-// pixels of its range for the batch, which keeps every pixel's fragments in one warp and in
-// submission order. Called by one warp.
+// Chooses how the tile's pixels are divided among the warps for one batch, by candidate-pixel
+// work: either interleaved rows (row r to warp r % kRasterWarps; suits scattered triangles) or
+// kRasterWarps contiguous column ranges of about equal work (suits runs of small triangles
+// along a screen row, which crowd into a few rows). Each warp then owns its pixels for the
+// batch, which keeps every pixel's fragments in one warp and in submission order. mode 0 =
+// rows, 1 = columns, own[] = the column range bounds. Called by one warp.
 template <int TS>
 __device__ __forceinline__ void split_work(const int* rowd, const int* cold, uint32_t* own,
-                                           uint32_t* axis_out) {
+                                           uint32_t* mode_out) {
     const uint32_t lane = lane_id();
-    uint32_t best = 0xFFFFFFFFu, best_axis = 0, best_part = 0;
-    for (uint32_t axis = 0; axis < 2; ++axis) {
-        const int* dd = axis == 0 ? rowd : cold;
-        int lw = lane < (uint32_t)TS ? dd[lane] : 0;
+    // per-line work from the difference arrays
+    int rw = lane < (uint32_t)TS ? rowd[lane] : 0, cw = lane < (uint32_t)TS ? cold[lane] : 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xFFFFFFFFu, lw, o);
-            if (lane >= (uint32_t)o) lw += y;
-        }
-        const uint32_t wl = lane < (uint32_t)TS ? (uint32_t)lw : 0u;  // work of line `lane`
-        uint32_t incl = wl;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
-        }
-        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        const uint32_t excl = incl - wl;
-        uint32_t part;
-        if (lane >= (uint32_t)TS) part = kRasterWarps;
-        else if (total == 0) part = lane * kRasterWarps / TS;
-        else part = min((uint32_t)(kRasterWarps - 1), ((2u * excl + wl) * kRasterWarps) / (2u * total));
-        uint32_t mx = 0;
-#pragma unroll
-        for (int k = 0; k < kRasterWarps; ++k)
-            mx = max(mx, __reduce_add_sync(0xFFFFFFFFu, part == (uint32_t)k ? wl : 0u));
-        if (mx < best) {
-            best = mx;
-            best_axis = axis;
-            best_part = part;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, rw, o), z = __shfl_up_sync(0xFFFFFFFFu, cw, o);
+        if (lane >= (uint32_t)o) {
+            rw += y;
+            cw += z;
         }
     }
+    const uint32_t wr = lane < (uint32_t)TS ? (uint32_t)rw : 0u;
+    const uint32_t wc = lane < (uint32_t)TS ? (uint32_t)cw : 0u;
+    // interleaved rows
+    uint32_t mrow = 0;
+#pragma unroll
+    for (int k = 0; k < kRasterWarps; ++k)
+        mrow = max(mrow, __reduce_add_sync(0xFFFFFFFFu, (lane % kRasterWarps) == (uint32_t)k ? wr : 0u));
+    // contiguous column ranges: a column goes to the range that holds the midpoint of its work
+    uint32_t incl = wc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t excl = incl - wc;
+    uint32_t part;
+    if (lane >= (uint32_t)TS) part = kRasterWarps;
+    else if (total == 0) part = lane * kRasterWarps / TS;
+    else part = min((uint32_t)(kRasterWarps - 1), ((2u * excl + wc) * kRasterWarps) / (2u * total));
+    uint32_t mcol = 0;
+#pragma unroll
+    for (int k = 0; k < kRasterWarps; ++k)
+        mcol = max(mcol, __reduce_add_sync(0xFFFFFFFFu, part == (uint32_t)k ? wc : 0u));
 #pragma unroll
     for (int k = 0; k <= kRasterWarps; ++k) {
-        const uint32_t b = __popc(__ballot_sync(0xFFFFFFFFu, best_part < (uint32_t)k));
-        if (lane == 0) own[k] = b;
+        const uint32_t bnd = __popc(__ballot_sync(0xFFFFFFFFu, part < (uint32_t)k));
+        if (lane == 0) own[k] = bnd;
     }
-    if (lane == 0) *axis_out = best_axis;
+    if (lane == 0) *mode_out = mcol < mrow ? 1u : 0u;
 }
 
 // Depth test, shading and colour write of up to 32 queued fragments of one warp (lane = one
@@ -819,7 +834,7 @@ __device__ __forceinline__ void clear_tile_warp(const FrameDev& f, uint32_t x0, 
 // mod.rs:225-253) — and depth-tests, shades and writes the covered fragments in order (C).
 // Bins without entries are then cleared by single warps from queue[1].
 template <int S, int TS>
-__global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __restrict__ frames,
+__global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __restrict__ frames,
                                                            int nframes,
                                                            const uint32_t* __restrict__ order,
                                                            uint32_t ntotal, uint32_t nsx,
@@ -851,8 +866,16 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
         sm.zb[i] = f.clear_depth;
         sm.cb[i] = kClearColor;
     }
-    const uint32_t nent = s.tile_count[gt];
-    const uint32_t* bins = s.bins + f.bin_base + s.tile_start[gt];
+    // the bin's entries, or for a quadrant of a 32-pixel bin its own split list
+    uint32_t nent;
+    const uint32_t* bins;
+    if (nsub > 1) {
+        nent = s.qcount[4ull * gt + sub];
+        bins = s.qbins + f.qbin_base + 4ull * s.tile_start[gt] + (unsigned long long)sub * s.tile_count[gt];
+    } else {
+        nent = s.tile_count[gt];
+        bins = s.bins + f.bin_base + s.tile_start[gt];
+    }
     const uint32_t mybit = 1u << sub;
 
     uint32_t pos = 0;  // next entry of the bin
@@ -869,14 +892,18 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             if (e < nent) {
                 const uint32_t ent = bins[e];
                 if (ent & mybit) {
-                    g = ent >> 4;
-                    aux = s.tri_aux[f.rect_base + g];
-                    nitems = (aux == kNone) ? 1u : (uint32_t)__float_as_int(s.clip_store[aux]) - 2u;
+                    g = ent >> kEntShift;
+                    nitems = 1;
+                    if (ent & kEntClipped) {
+                        aux = s.tri_aux[f.rect_base + g];
+                        nitems = (uint32_t)__float_as_int(s.clip_store[aux]) - 2u;
+                    }
                 }
             }
             if (threadIdx.x == 0) sm.misc[1] = nit;
             uint32_t itot;
             const uint32_t iex = block_excl_scan(nitems, sm.tmp, itot);
+            // entries fit while the running item count stays within the batch (a prefix)
             const bool part = (e < nent) && (nit + iex + nitems <= (uint32_t)C::IC);
             const uint32_t take = __syncthreads_count(part);
             if (part && threadIdx.x == take - 1) sm.misc[1] = nit + iex + nitems;
@@ -887,21 +914,32 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             pos += take;
             if (take < window) break;  // the batch is full
         }
-        // ---- B. split rows or columns over the warps; which warps each item reaches
+        // ---- B. divide the tile's pixels among the warps; which warps each item reaches
         if (warp == 0) split_work<TS>(sm.rowd, sm.cold, sm.own, &sm.misc[5]);
         __syncthreads();
-        const uint32_t axis = sm.misc[5];
+        const uint32_t mode = sm.misc[5];
         {
             const uint32_t t = threadIdx.x;
             uint32_t wm = 0;
             if (t < nit) {
                 const uint32_t r = sm.irect[t];
-                const uint32_t a0 = axis ? (r & 0xFFu) : ((r >> 8) & 0xFFu);
-                const uint32_t a1 = axis ? ((r >> 16) & 0xFFu) : (r >> 24);
-                if (a1 > a0) {
+                if (mode == 0) {
+                    // interleaved rows: warps of rows ly0 .. ly1 - 1
+                    const uint32_t ly0 = (r >> 8) & 0xFFu, ly1 = r >> 24;
+                    if (ly1 > ly0) {
+                        const uint32_t nrow = ly1 - ly0;
+                        wm = nrow >= (uint32_t)kRasterWarps
+                                 ? (1u << kRasterWarps) - 1u
+                                 : (((1u << nrow) - 1u) << (ly0 % kRasterWarps));
+                        wm = (wm | (wm >> kRasterWarps)) & ((1u << kRasterWarps) - 1u);
+                    }
+                } else {
+                    const uint32_t a0 = r & 0xFFu, a1 = (r >> 16) & 0xFFu;
+                    if (a1 > a0) {
 #pragma unroll
-                    for (int w = 0; w < kRasterWarps; ++w)
-                        if (a0 < sm.own[w + 1] && a1 > sm.own[w]) wm |= 1u << w;
+                        for (int w = 0; w < kRasterWarps; ++w)
+                            if (a0 < sm.own[w + 1] && a1 > sm.own[w]) wm |= 1u << w;
+                    }
                 }
             }
 #pragma unroll
@@ -914,6 +952,7 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
         // ---- C. per warp, in submission order: candidate pixels of its range, coverage and
         // sample depths, then ordered depth test and shading of the covered fragments
         const uint32_t olo = sm.own[warp], ohi = sm.own[warp + 1];
+        const uint32_t rstep = mode == 0 ? (uint32_t)kRasterWarps : 1u;
         uint32_t nmine = 0;
 #pragma unroll
         for (int src = 0; src < C::IC / 32; ++src) {
@@ -930,17 +969,21 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
             if (act) {
                 const uint32_t r = sm.irect[it_l];
                 uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
-                if (axis) {
+                uint32_t nrows;
+                if (mode == 0) {
+                    // first row of the box owned by this warp, then every kRasterWarps-th row
+                    const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
+                    nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
+                    ly0 = first;
+                } else {
                     lx0 = max(lx0, olo);
                     lx1 = min(lx1, ohi);
-                } else {
-                    ly0 = max(ly0, olo);
-                    ly1 = min(ly1, ohi);
+                    nrows = ly1 - ly0;
                 }
                 cx0 = lx0;
                 cw = lx1 - lx0;
                 cy0 = ly0;
-                c = cw * (ly1 - ly0);
+                c = cw * nrows;
             }
             uint32_t incl = c;
 #pragma unroll
@@ -970,7 +1013,7 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
                 for (int k = 0; k < S; ++k) z[k] = 0.0f;
                 if (p < total) {
                     const uint32_t rr = p - exc;
-                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + rr / sw;
+                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + rstep * (rr / sw);
                     pix = ly * TS + lx;
                     const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
                     float n0x, n0y, n1x, n1y, n2x, n2y;
@@ -1072,6 +1115,57 @@ __global__ void __launch_bounds__(kRasterThreads, 3) k_raster(const FrameDev* __
     }
 }
 
+// Splits each 32-pixel bin of a raster launch into its four quadrant lists, keeping submission
+// order within each (an entry goes to every quadrant its mask names). One CTA per bin; the
+// quadrant raster CTAs then read only their own entries.
+__global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ frames, int nframes,
+                                                   uint32_t tile0, Scratch s) {
+    __shared__ uint32_t wcnt[4][8];
+    __shared__ uint32_t base[4];
+    const uint32_t gt = tile0 + blockIdx.x;
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+    const bool overflow = (*(volatile const uint32_t*)s.status & ST_BIN_OVERFLOW) != 0;
+    const uint32_t n = overflow ? 0u : s.tile_count[gt];
+    if (threadIdx.x < 4) {
+        s.qcount[4ull * gt + threadIdx.x] = 0;
+        base[threadIdx.x] = 0;
+    }
+    if (n == 0) return;
+    const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
+    const unsigned long long start = s.tile_start[gt];
+    const uint32_t* src = s.bins + f.bin_base + start;
+    uint32_t* dst = s.qbins + f.qbin_base + 4ull * start;
+    __syncthreads();
+    for (uint32_t e0 = 0; e0 < n; e0 += blockDim.x) {
+        const uint32_t e = e0 + threadIdx.x;
+        const uint32_t ent = e < n ? src[e] : 0u;
+        uint32_t rank[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t b = __ballot_sync(0xFFFFFFFFu, (ent >> q) & 1u);
+            rank[q] = __popc(b & lanemask_lt());
+            if (lane == 0) wcnt[q][warp] = __popc(b);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if ((ent >> q) & 1u) {
+                uint32_t off = base[q] + rank[q];
+                for (uint32_t w = 0; w < warp; ++w) off += wcnt[q][w];
+                dst[(unsigned long long)q * n + off] = ent;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            uint32_t t = 0;
+            for (uint32_t w = 0; w < blockDim.x / 32; ++w) t += wcnt[threadIdx.x][w];
+            base[threadIdx.x] += t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) s.qcount[4ull * gt + threadIdx.x] = base[threadIdx.x];
+}
+
 // Tile queue of one raster launch: tiles with entries first, in decreasing order of entry
 // count (bucketed by bit length), then tiles without entries; queue[2] = tiles with entries.
 // One block.
@@ -1124,6 +1218,9 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         grid_cap = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
+    if (nsx > 1)
+        k_bin_split<<<a.raster_blocks, 256, 0, a.stream>>>(a.raster_frames, a.raster_nframes,
+                                                           a.raster_tile_offset, a.scratch);
     k_tile_order<<<1, 1024, 0, a.stream>>>(a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
                                            a.scratch.tile_order, a.raster_queue, a.scratch.status);
     const unsigned long long units = (unsigned long long)a.raster_blocks * nsx * nsx;

@@ -149,6 +149,10 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     const size_t o_torder = c.take(sizeof(uint32_t) * F.ntiles);
     const size_t o_need = c.take(sizeof(unsigned long long));
     const size_t o_bins = c.take(sizeof(uint32_t) * F.bin_cap);
+    // 32-pixel bins are split into quadrant lists for the raster
+    const bool split = raster_edge(ts) < ts;
+    const size_t o_qbins = c.take(split ? sizeof(uint32_t) * 4ull * F.bin_cap : 0);
+    const size_t o_qcount = c.take(split ? sizeof(uint32_t) * 4ull * F.ntiles : 0);
     const size_t clip_floats = 32ull * ntris + 4096ull;
     const size_t o_clip = c.take(sizeof(float) * clip_floats);
     if (c.off > kNoAllocScratchBytes) return RAST_INVALID_ARG;
@@ -210,6 +214,8 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     S.tile_count = reinterpret_cast<uint32_t*>(base + o_tcount);
     S.tile_order = reinterpret_cast<uint32_t*>(base + o_torder);
     S.bins = reinterpret_cast<uint32_t*>(base + o_bins);
+    S.qbins = split ? reinterpret_cast<uint32_t*>(base + o_qbins) : nullptr;
+    S.qcount = split ? reinterpret_cast<uint32_t*>(base + o_qcount) : nullptr;
     S.clip_store = reinterpret_cast<float*>(base + o_clip);
     S.clip_cap = clip_floats;
     S.clip_used = &dstate->clip_used;

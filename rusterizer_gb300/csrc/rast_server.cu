@@ -51,7 +51,7 @@ struct Slot {
 using ShapeKey = std::tuple<uint32_t, int, int, int, int>;  // mesh, width, height, msaa, tile
 
 // Device bytes a scene needs while in flight: vertex records, per-triangle rectangles, chunk
-// histograms, tile tables, bins, clip store and its image.
+// histograms, tile tables, bins (and quadrant lists for 32-pixel bins), clip store and its image.
 uint64_t footprint_of(const rast_ctx* c, const rast_scene& s, int ts, uint64_t bins) {
     const MeshRec& m = c->meshes[s.mesh];
     const uint64_t tiles = (uint64_t)((s.width + ts - 1) / ts) * ((s.height + ts - 1) / ts);
@@ -59,7 +59,8 @@ uint64_t footprint_of(const rast_ctx* c, const rast_scene& s, int ts, uint64_t b
     cs = std::min<uint64_t>(std::max<uint64_t>((cs + 255u) & ~255ull, 512u), 8192u);
     const uint64_t chunks = (m.ntris + cs - 1) / cs;
     const uint64_t bin_cap = std::max<uint64_t>(bins, 4ull * m.ntris + tiles + 1024ull);
-    return 34ull * m.nverts + 12ull * m.ntris + 4ull * chunks * tiles + 12ull * tiles + 4ull * bin_cap +
+    const uint64_t split = raster_edge(ts) < ts ? 16ull * (bin_cap + tiles) : 0ull;
+    return 34ull * m.nverts + 12ull * m.ntris + 4ull * chunks * tiles + 12ull * tiles + 4ull * bin_cap + split +
            4ull * (32ull * m.ntris + 4096ull) + 4ull * (uint64_t)s.width * s.height + 65536ull;
 }
 

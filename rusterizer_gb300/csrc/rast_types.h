@@ -12,8 +12,10 @@
 //   tri_aux[t]  u32   offset of the clipped polygon in clip_store, kNone when unclipped
 //   counts[frame][chunk][tile] u32  per-chunk tile histograms, then exclusive prefixes
 //   tile_start / tile_count [tile]  each tile's bin range
-//   bins[]    u32     per-tile lists in submission order: triangle << 4 | mask of the
-//                     raster quadrants of the bin that its pixel box touches
+//   bins[]    u32     per-tile lists in submission order: triangle << 5 | clipped << 4 |
+//                     mask of the raster quadrants of the bin that its pixel box touches
+//   qbins[]   u32     32-pixel bins only: each bin's entries split into its four 16-pixel
+//                     quadrants (stable), quadrant q of bin t at 4 * start(t) + q * count(t)
 // Per-sample colour and depth never touch HBM: they live in shared memory of the tile CTA.
 #pragma once
 
@@ -27,7 +29,10 @@ constexpr int kMaxPoly = 32;                   // clip polygon capacity (a conve
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kRectEmpty = ~0ull;
 constexpr int kMaxTilesPerFrame = 16384;       // per-frame tile count limit (smem histograms)
-constexpr uint32_t kMaxFrameTris = 1u << 28;     // bin entries hold triangle << 4 | quadrant mask
+// bin entries: triangle << 5 | clipped << 4 | mask of the raster quadrants the box touches
+constexpr int kEntShift = 5;
+constexpr uint32_t kEntClipped = 1u << 4;
+constexpr uint32_t kMaxFrameTris = 1u << (32 - kEntShift);
 
 // Edge of the raster tile that one CTA owns for bins of edge ts: 32-pixel bins are rastered as
 // four 16-pixel quadrants (more, smaller units balance the persistent raster kernel better).
@@ -82,6 +87,7 @@ struct FrameDev {
     unsigned long long count_base;  // offset of counts[frame]
     unsigned long long bin_base;    // offset of this frame's bins
     unsigned long long bin_cap;     // bins reserved for this frame
+    unsigned long long qbin_base;   // offset of this frame's quadrant lists (32-pixel bins)
     float clear_depth;
     uint32_t* out;         // width * height ARGB (device)
     float* dbg_depth;      // optional [y][x][s]
@@ -106,6 +112,8 @@ struct Scratch {
     uint32_t* tile_count;
     uint32_t* tile_order;               // raster queue: tiles by decreasing entry count
     uint32_t* bins;
+    uint32_t* qbins;                    // per 32-pixel bin: its entries split by raster quadrant
+    uint32_t* qcount;                   // [4 * tile + quadrant] entries in each quadrant list
     float* clip_store;
     unsigned long long clip_cap;        // floats
     unsigned long long* clip_used;      // floats allocated this frame
