@@ -507,7 +507,8 @@ struct RasterCfg {
     static constexpr int NPIX = TS * TS;
     static constexpr int IC = kRasterThreads;  // items (triangles after clipping) per batch
     static constexpr int QC = 64;              // per-warp fragment ring
-    static_assert(TS <= 32, "one lane per tile row or column in the work split");
+    static_assert(TS <= 16 && IC <= 256, "ring entries hold item and pixel in one byte each");
+    static_assert(TS <= 2 * kRasterWarps, "row mode gives a warp at most two rows of a tile");
 };
 
 template <int S, int TS>
@@ -517,7 +518,7 @@ struct RasterSmem {
     uint32_t cb[C::NPIX * S];
     // items of the current batch (struct of arrays)
     float ipx[3][C::IC], ipy[3][C::IC], iz[3][C::IC], iw[3][C::IC], iinv[C::IC];
-    float iat[12][C::IC];  // uv (6 floats) or colour (12 floats), per the draw's shader
+    float iuv[6][C::IC];  // texture coordinates (u, v) of the three corners
     uint32_t irect[C::IC];  // tile-local pixel box: x0 | y0 << 8 | x1 << 16 | y1 << 24
     uint32_t itri[C::IC];
     uint32_t imeta[C::IC];  // draw << 8 | sub-triangle
@@ -525,9 +526,14 @@ struct RasterSmem {
     uint16_t wlist[kRasterWarps][C::IC];         // the warp's items, in submission order
     // per-warp rings of covered fragments, in submission order
     float qz[kRasterWarps][S][C::QC];
-    uint16_t qitem[kRasterWarps][C::QC];
-    uint16_t qpix[kRasterWarps][C::QC];
+    uint8_t qitem[kRasterWarps][C::QC];
+    uint8_t qpix[kRasterWarps][C::QC];
     uint8_t qcov[kRasterWarps][C::QC];
+    // per-warp rings of depth-passed fragments waiting for the fragment shader, in order
+    float sz0[kRasterWarps][C::QC];
+    uint8_t sitem[kRasterWarps][C::QC];
+    uint8_t spix[kRasterWarps][C::QC];
+    uint8_t sdm[kRasterWarps][C::QC];
     float inv255[256];
     int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
     uint32_t own[kRasterWarps + 1];  // column mode: warp w owns columns [own[w], own[w+1])
@@ -571,6 +577,59 @@ __device__ __forceinline__ void item_normal(const RasterSmem<S, TS>& sm, uint32_
     ny = vx;
 }
 
+// The pixels of one line of an item's box that can hold a covered sample: line lc (a tile-local
+// row in mode 0, a column in mode 1), candidates [a0, a1) along it, trimmed in place. A pixel is
+// dropped only where some edge k is negative at every sample with room to spare: with E_k the
+// edge function in exact arithmetic over the stored f32 normal and point, the computed
+// edge_eval value differs from E_k by at most 3 * 2^-24 * (|nx| |x - Px| + |ny| |y - Py|)
+// (two subtractions, two products and one sum, each correctly rounded; the leading 0 + is
+// exact), so E_k(centre) + 3/8 (|nx| + |ny|) + m_k < 0, m_k = 1e-6 (|nx| (|Px| + 16400) +
+// |ny| (|Py| + 16400)) + 1e-37, makes every sample's computed value negative, and the edge
+// test fails whatever the tie rule (screen coordinates stay below 16400). The threshold along
+// the line is computed in f32 and widened by a pixel on each side. Non-finite points are not
+// trimmed.
+template <int S, int TS>
+__device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t it, uint32_t mode, uint32_t lc,
+                                          uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
+    const float px[3] = {sm.ipx[0][it], sm.ipx[1][it], sm.ipx[2][it]};
+    const float py[3] = {sm.ipy[0][it], sm.ipy[1][it], sm.ipy[2][it]};
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) finite = finite && isfinite(px[k]) && isfinite(py[k]);
+    if (!finite) return;
+    const float rs = S == 1 ? 0.0f : 0.375f;
+    // line centre across, and the pixel-centre origin along the line (global coordinates)
+    const float cacross = (float)((mode == 0 ? Y0 : X0) + lc) + 0.5f;
+    const float oalong = (float)(mode == 0 ? X0 : Y0) + 0.5f;
+    int lo = (int)a0, hi = (int)a1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int n = k == 2 ? 0 : k + 1;
+        const float nx = -(py[n] - py[k]), ny = px[n] - px[k];
+        const float R = rs * (fabsf(nx) + fabsf(ny)) +
+                        1e-6f * (fabsf(nx) * (fabsf(px[k]) + 16400.0f) + fabsf(ny) * (fabsf(py[k]) + 16400.0f)) +
+                        1e-37f;
+        const float nal = mode == 0 ? nx : ny, nac = mode == 0 ? ny : nx;
+        const float pal = mode == 0 ? px[k] : py[k], pac = mode == 0 ? py[k] : px[k];
+        const float gk = nac * (cacross - pac) + R;  // E_k + R = nal * (c_along - pal) + gk
+        if (fabsf(nal) <= 1e-20f) {
+            // (almost) constant along the line
+            if (gk + fabsf(nal) * (fabsf(pal) + 16400.0f) < 0.0f) hi = lo;
+            continue;
+        }
+        // E_k + R >= 0  <=>  nal * (oalong + x - pal) >= -gk
+        const float t = pal - __fdividef(gk, nal) - oalong;  // widened below: 2-ulp division is enough
+        if (!isfinite(t)) continue;
+        const float tc = fminf(fmaxf(t, -8.0f), (float)TS + 8.0f);
+        const int ti = (int)floorf(tc);
+        if (nal > 0.0f) lo = max(lo, ti - 1);
+        else hi = min(hi, ti + 2);
+    }
+    if (hi < lo) hi = lo;
+    a0 = (uint32_t)lo;
+    a1 = (uint32_t)hi;
+}
+
 // Stages the items of one bin entry (one triangle, or the fan of its clipped polygon) at
 // positions first.. of the batch: screen points, depths, w, attributes, 1 / 2x area and the
 // tile-local pixel box, and adds the box to the batch's row and column work.
@@ -585,7 +644,7 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
     for (uint32_t k = 0; k < nitems; ++k) {
         const uint32_t it = first + k;
         float4 sv[3];
-        float at[3][6];
+        float uv[3][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
         if (aux == kNone) {
             const uint32_t tri = g - d.tbase;
             const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
@@ -593,17 +652,9 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 sv[q] = s.vscr[d.vbase + ii[q]];
-                if (fs == 1) {
-                    if (d.rgba) {
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) at[q][c] = __ldg(d.rgba + 4ull * ii[q] + c);
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) at[q][c] = 0.0f;
-                    }
-                } else if (fs == 0) {
-                    at[q][4] = __ldg(d.uv + 2ull * ii[q]);
-                    at[q][5] = __ldg(d.uv + 2ull * ii[q] + 1);
+                if (fs == 0) {
+                    uv[q][0] = __ldg(d.uv + 2ull * ii[q]);
+                    uv[q][1] = __ldg(d.uv + 2ull * ii[q] + 1);
                 }
             }
         } else {
@@ -613,8 +664,8 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
             for (int q = 0; q < 3; ++q) {
                 const float* o = st + 10 * vi[q];
                 sv[q] = make_float4(o[0], o[1], o[2], o[3]);
-#pragma unroll
-                for (int c = 0; c < 6; ++c) at[q][c] = o[4 + c];
+                uv[q][0] = o[8];
+                uv[q][1] = o[9];
             }
         }
 #pragma unroll
@@ -623,13 +674,8 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
             sm.ipy[q][it] = sv[q].y;
             sm.iz[q][it] = sv[q].z;
             sm.iw[q][it] = sv[q].w;
-            if (fs == 0) {
-                sm.iat[2 * q][it] = at[q][4];
-                sm.iat[2 * q + 1][it] = at[q][5];
-            } else if (fs == 1) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c) sm.iat[4 * q + c][it] = at[q][c];
-            }
+            sm.iuv[2 * q][it] = uv[q][0];
+            sm.iuv[2 * q + 1][it] = uv[q][1];
         }
         // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
         sm.iinv[it] = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
@@ -706,15 +752,37 @@ __device__ __forceinline__ void split_work(const int* rowd, const int* cold, uin
     if (lane == 0) *mode_out = mcol < mrow ? 1u : 0u;
 }
 
-// Depth test, shading and colour write of up to 32 queued fragments of one warp (lane = one
-// fragment, queue order = submission order). Fragments of the same pixel run in rounds of
-// increasing rank, so both the depth test (depth_coverage, src/rasterizer/mod.rs:363-378) and
-// the sample writes (write_pixel, mod.rs:380-397) happen in submission order.
+// FS::Color's input for an item: the vertex colours of its three corners (Color vertex
+// attribute, src/graphics_primitives.rs:9-13), from the mesh or from the clipped polygon.
+__device__ __forceinline__ void item_colours(const DrawDev& d, const FrameDev& f, const Scratch& s, uint32_t g,
+                                             uint32_t k, float col[3][4]) {
+    const uint32_t aux = s.tri_aux[f.rect_base + g];
+    if (aux == kNone) {
+        const uint32_t tri = g - d.tbase;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const uint32_t vi = __ldg(d.idx + 3ull * tri + q);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) col[q][c] = d.rgba ? __ldg(d.rgba + 4ull * vi + c) : 0.0f;
+        }
+    } else {
+        const float* st = s.clip_store + aux + 1;
+        const uint32_t vi[3] = {0u, k + 1, k + 2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) col[q][c] = st[10 * vi[q] + 4 + c];
+    }
+}
+
+// Depth test of up to 32 queued fragments of one warp (lane = one fragment, queue order =
+// submission order). Fragments of the same pixel run in rounds of increasing rank, so the
+// depth test (depth_coverage, src/rasterizer/mod.rs:363-378) happens in submission order.
+// Fragments with samples that passed go, in the same order, to the warp's shade ring.
 template <int S, int TS>
-__device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head,
-                                             uint32_t n, const DrawDev* __restrict__ draws,
-                                             const Scratch& s, uint32_t X0, uint32_t Y0,
-                                             uint32_t& shaded, uint32_t& fsinv, uint32_t& oobc) {
+__device__ __forceinline__ void warp_depth(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head, uint32_t n,
+                                           uint32_t& stail, const Scratch& s, uint32_t X0, uint32_t Y0,
+                                           uint32_t& shaded, uint32_t& fsinv) {
     using C = RasterCfg<S, TS>;
     const uint32_t lane = lane_id();
     const bool valid = lane < n;
@@ -758,9 +826,37 @@ __device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, 
         }
         __syncwarp();
     }
-    uint32_t argb = 0;
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, dm != 0);
     if (dm) {
-        // Fragment::interpolate (src/rasterizer/mod.rs:69-100), then the fragment shader
+        const uint32_t sq = (stail + __popc(bal & lanemask_lt())) & (C::QC - 1);
+        sm.sitem[w][sq] = (uint8_t)it;
+        sm.spix[w][sq] = (uint8_t)pix;
+        sm.sdm[w][sq] = (uint8_t)dm;
+        sm.sz0[w][sq] = z[0];
+        shaded += __popc(dm);
+        fsinv += 1;
+    }
+    stail += __popc(bal);
+    __syncwarp();
+}
+
+// Fragment shader and colour write of up to 32 fragments of the warp's shade ring:
+// Fragment::interpolate (src/rasterizer/mod.rs:69-100) at the point its depth-passed mask
+// selects, the draw's shader by id, then write_pixel (mod.rs:380-397) to the passed samples,
+// same-pixel fragments in rounds of increasing rank (submission order).
+template <int S, int TS>
+__device__ __forceinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head, uint32_t n,
+                                           const DrawDev* __restrict__ draws, const FrameDev& f,
+                                           const Scratch& s, uint32_t X0, uint32_t Y0, uint32_t& oobc) {
+    using C = RasterCfg<S, TS>;
+    const uint32_t lane = lane_id();
+    const bool valid = lane < n;
+    const uint32_t q = (head + lane) & (C::QC - 1);
+    uint32_t argb = 0, pix = 0, dm = 0;
+    if (valid) {
+        const uint32_t it = sm.sitem[w][q];
+        pix = sm.spix[w][q];
+        dm = sm.sdm[w][q];
         const uint32_t x = X0 + pix % TS, y = Y0 + pix / TS;
         float xs, ys;
         interp_point<S>(x, y, dm, xs, ys);
@@ -777,29 +873,33 @@ __device__ __forceinline__ void warp_process(RasterSmem<S, TS>& sm, uint32_t w, 
         float col[4];
         if (d.fs == 0) {
             // FS::Texture (upstream src/main.rs:214-216)
-            const float tu = sm.iat[0][it] * u + sm.iat[2][it] * v + sm.iat[4][it] * ww;
-            const float tv = sm.iat[1][it] * u + sm.iat[3][it] * v + sm.iat[5][it] * ww;
+            const float tu = sm.iuv[0][it] * u + sm.iuv[2][it] * v + sm.iuv[4][it] * ww;
+            const float tv = sm.iuv[1][it] * u + sm.iuv[3][it] * v + sm.iuv[5][it] * ww;
             bool oob = false;
             tex_sample(d.tex, d.tex_w, d.tex_h, tu, tv, sm.inv255, col, oob);
             if (oob) ++oobc;
         } else if (d.fs == 1) {
             // FS::Color (upstream src/main.rs:217)
+            float vc[3][4];
+            item_colours(d, f, s, sm.itri[it], sm.imeta[it] & 0xFFu, vc);
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-                col[c] = sm.iat[c][it] * u + sm.iat[4 + c][it] * v + sm.iat[8 + c][it] * ww;
+            for (int c = 0; c < 4; ++c) col[c] = vc[0][c] * u + vc[1][c] * v + vc[2][c] * ww;
         } else {
             // FS::Debug (upstream src/main.rs:218-220): grayscale(frag_coords.depths[0])
-            col[0] = z[0];
-            col[1] = z[0];
-            col[2] = z[0];
+            const float z0 = sm.sz0[w][q];
+            col[0] = z0;
+            col[1] = z0;
+            col[2] = z0;
             col[3] = 1.0f;
         }
         argb = to_argb(col[0], col[1], col[2], col[3]);
-        shaded += __popc(dm);
-        fsinv += 1;
     }
+    const uint32_t key = valid ? pix : 0x10000u + lane;
+    const uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t rank = __popc(grp & lanemask_lt());
+    const uint32_t maxr = __reduce_max_sync(0xFFFFFFFFu, rank);
     for (uint32_t r = 0; r <= maxr; ++r) {
-        if (dm && rank == r) {
+        if (valid && rank == r) {
 #pragma unroll
             for (int k = 0; k < S; ++k)
                 if ((dm >> k) & 1u) sm.cb[pix * S + k] = argb;
@@ -949,10 +1049,12 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             }
         }
         __syncthreads();
-        // ---- C. per warp, in submission order: candidate pixels of its range, coverage and
-        // sample depths, then ordered depth test and shading of the covered fragments
+        // ---- C. per warp, in submission order: the candidate pixels of its items inside its
+        // range (in row mode each of an item's rows trimmed to the pixels that can hold a
+        // covered sample, line_span); coverage (EdgeFunctions::eval, mod.rs:134-146) and
+        // sample depths (RasterizerTriangle::fragment, mod.rs:225-253) of each; then ordered
+        // depth test and shading of the covered fragments
         const uint32_t olo = sm.own[warp], ohi = sm.own[warp + 1];
-        const uint32_t rstep = mode == 0 ? (uint32_t)kRasterWarps : 1u;
         uint32_t nmine = 0;
 #pragma unroll
         for (int src = 0; src < C::IC / 32; ++src) {
@@ -961,29 +1063,35 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             nmine += __popc(bits);
         }
         __syncwarp();
-        uint32_t head = 0, tail = 0;
+        uint32_t head = 0, tail = 0, shead = 0, stail = 0;
         for (uint32_t gb = 0; gb < nmine; gb += 32) {
             const bool act = gb + lane < nmine;
             const uint32_t it_l = act ? sm.wlist[warp][gb + lane] : 0u;
-            uint32_t cx0 = 0, cw = 1, cy0 = 0, c = 0;
+            // candidates of the lane's item and where they lie:
+            //   row mode:    first row | first-row start << 5 | first-row length << 10 |
+            //                second-row start << 15 (second row = first + kRasterWarps)
+            //   column mode: x0 | y0 << 5 | width << 10 | ceil(65536 / width) << 15
+            uint32_t c = 0, geo = 0;
             if (act) {
                 const uint32_t r = sm.irect[it_l];
-                uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
-                uint32_t nrows;
+                const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
                 if (mode == 0) {
-                    // first row of the box owned by this warp, then every kRasterWarps-th row
                     const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
-                    nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
-                    ly0 = first;
+                    const uint32_t nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
+                    uint32_t s1 = lx0, e1 = lx1, s2 = lx0, e2 = lx1;
+                    if (nrows > 0 && lx1 - lx0 >= 4) {
+                        line_span<S, TS>(sm, it_l, 0u, first, X0, Y0, s1, e1);
+                        if (nrows > 1) line_span<S, TS>(sm, it_l, 0u, first + kRasterWarps, X0, Y0, s2, e2);
+                    }
+                    const uint32_t w1 = nrows > 0 ? e1 - s1 : 0u, w2 = nrows > 1 ? e2 - s2 : 0u;
+                    c = w1 + w2;
+                    geo = first | (s1 << 5) | (w1 << 10) | (s2 << 15);
                 } else {
-                    lx0 = max(lx0, olo);
-                    lx1 = min(lx1, ohi);
-                    nrows = ly1 - ly0;
+                    const uint32_t cx0 = max(lx0, olo), cx1 = min(lx1, ohi);
+                    const uint32_t sw = cx1 > cx0 ? cx1 - cx0 : 1u;
+                    c = cx1 > cx0 ? sw * (ly1 - ly0) : 0u;
+                    geo = cx0 | (ly0 << 5) | (sw << 10) | (((65535u + sw) / sw) << 15);
                 }
-                cx0 = lx0;
-                cw = lx1 - lx0;
-                cy0 = ly0;
-                c = cw * nrows;
             }
             uint32_t incl = c;
 #pragma unroll
@@ -1004,16 +1112,25 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 const uint32_t sj = min(j, 31u);
                 const uint32_t it = __shfl_sync(0xFFFFFFFFu, it_l, sj);
                 const uint32_t exc = __shfl_sync(0xFFFFFFFFu, incl - c, sj);
-                const uint32_t sx0 = __shfl_sync(0xFFFFFFFFu, cx0, sj);
-                const uint32_t sw = __shfl_sync(0xFFFFFFFFu, cw, sj);
-                const uint32_t sy0 = __shfl_sync(0xFFFFFFFFu, cy0, sj);
+                const uint32_t gg = __shfl_sync(0xFFFFFFFFu, geo, sj);
                 uint32_t cov = 0, pix = 0;
                 float z[S];
 #pragma unroll
                 for (int k = 0; k < S; ++k) z[k] = 0.0f;
                 if (p < total) {
                     const uint32_t rr = p - exc;
-                    const uint32_t lx = sx0 + rr % sw, ly = sy0 + rstep * (rr / sw);
+                    uint32_t lx, ly;
+                    if (mode == 0) {
+                        const uint32_t w1 = (gg >> 10) & 31u;
+                        const bool second = rr >= w1;
+                        lx = second ? ((gg >> 15) & 31u) + (rr - w1) : ((gg >> 5) & 31u) + rr;
+                        ly = (gg & 31u) + (second ? (uint32_t)kRasterWarps : 0u);
+                    } else {
+                        // rr / width by multiply-shift: exact while rr * width < 65536 (rr < 256)
+                        const uint32_t sw = (gg >> 10) & 31u, q = (rr * (gg >> 15)) >> 16;
+                        lx = (gg & 31u) + rr - q * sw;
+                        ly = ((gg >> 5) & 31u) + q;
+                    }
                     pix = ly * TS + lx;
                     const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
                     float n0x, n0y, n1x, n1y, n2x, n2y;
@@ -1046,8 +1163,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 const uint32_t bal = __ballot_sync(0xFFFFFFFFu, cov != 0);
                 if (cov) {
                     const uint32_t q = (tail + __popc(bal & lanemask_lt())) & (C::QC - 1);
-                    sm.qitem[warp][q] = (uint16_t)it;
-                    sm.qpix[warp][q] = (uint16_t)pix;
+                    sm.qitem[warp][q] = (uint8_t)it;
+                    sm.qpix[warp][q] = (uint8_t)pix;
                     sm.qcov[warp][q] = (uint8_t)cov;
 #pragma unroll
                     for (int k = 0; k < S; ++k) sm.qz[warp][k][q] = z[k];
@@ -1055,12 +1172,21 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 tail += __popc(bal);
                 __syncwarp();
                 if (tail - head >= 32) {
-                    warp_process<S, TS>(sm, warp, head, 32, draws, s, X0, Y0, shaded, fsinv, oobc);
+                    warp_depth<S, TS>(sm, warp, head, 32, stail, s, X0, Y0, shaded, fsinv);
                     head += 32;
+                    if (stail - shead >= 32) {
+                        warp_shade<S, TS>(sm, warp, shead, 32, draws, f, s, X0, Y0, oobc);
+                        shead += 32;
+                    }
                 }
             }
         }
-        if (tail != head) warp_process<S, TS>(sm, warp, head, tail - head, draws, s, X0, Y0, shaded, fsinv, oobc);
+        if (tail != head) warp_depth<S, TS>(sm, warp, head, tail - head, stail, s, X0, Y0, shaded, fsinv);
+        while (stail != shead) {
+            const uint32_t nsh = min(stail - shead, 32u);
+            warp_shade<S, TS>(sm, warp, shead, nsh, draws, f, s, X0, Y0, oobc);
+            shead += nsh;
+        }
         __syncthreads();
     }
 
