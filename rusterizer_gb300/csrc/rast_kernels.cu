@@ -514,7 +514,7 @@ struct RasterCfg {
 template <int S, int TS>
 struct RasterSmem {
     using C = RasterCfg<S, TS>;
-    float zb[C::NPIX * S];
+    float zb[C::NPIX * S];     // sample-major: sample k of pixel p at k * NPIX + p
     uint32_t cb[C::NPIX * S];
     // items of the current batch (struct of arrays)
     float ipx[3][C::IC], ipy[3][C::IC], iz[3][C::IC], iw[3][C::IC], iinv[C::IC];
@@ -752,10 +752,25 @@ __device__ __forceinline__ void split_work(const int* rowd, const int* cold, uin
     if (lane == 0) *mode_out = mcol < mrow ? 1u : 0u;
 }
 
+// Appends one fragment record to the debug log (rast_debug_log_enable); kept out of line.
+__device__ __noinline__ void log_fragment(const Scratch& s, uint32_t tri, uint32_t sub, uint32_t yx,
+                                          uint32_t masks) {
+    const unsigned long long slot = atomicAdd(s.log_n, 1ull);
+    if (slot < s.log_cap) {
+        uint32_t* L = s.log + 4ull * slot;
+        L[0] = tri;
+        L[1] = sub;
+        L[2] = yx;
+        L[3] = masks;
+    } else {
+        atomicOr(s.status, ST_LOG_OVERFLOW);
+    }
+}
+
 // FS::Color's input for an item: the vertex colours of its three corners (Color vertex
 // attribute, src/graphics_primitives.rs:9-13), from the mesh or from the clipped polygon.
-__device__ __forceinline__ void item_colours(const DrawDev& d, const FrameDev& f, const Scratch& s, uint32_t g,
-                                             uint32_t k, float col[3][4]) {
+__device__ __noinline__ void item_colours(const DrawDev& d, const FrameDev& f, const Scratch& s, uint32_t g,
+                                          uint32_t k, float col[3][4]) {
     const uint32_t aux = s.tri_aux[f.rect_base + g];
     if (aux == kNone) {
         const uint32_t tri = g - d.tbase;
@@ -807,22 +822,13 @@ __device__ __forceinline__ void warp_depth(RasterSmem<S, TS>& sm, uint32_t w, ui
         if (valid && rank == r) {
 #pragma unroll
             for (int k = 0; k < S; ++k)
-                if (((cov >> k) & 1u) && z[k] < sm.zb[pix * S + k]) {
+                if (((cov >> k) & 1u) && z[k] < sm.zb[k * C::NPIX + pix]) {
                     dm |= 1u << k;
-                    sm.zb[pix * S + k] = z[k];
+                    sm.zb[k * C::NPIX + pix] = z[k];
                 }
-            if (s.log) {
-                const unsigned long long slot = atomicAdd(s.log_n, 1ull);
-                if (slot < s.log_cap) {
-                    uint32_t* L = s.log + 4ull * slot;
-                    L[0] = sm.itri[it];
-                    L[1] = sm.imeta[it] & 0xFFu;
-                    L[2] = ((Y0 + pix / TS) << 16) | (X0 + pix % TS);
-                    L[3] = (dm << 8) | cov;
-                } else {
-                    atomicOr(s.status, ST_LOG_OVERFLOW);
-                }
-            }
+            if (s.log)
+                log_fragment(s, sm.itri[it], sm.imeta[it] & 0xFFu, ((Y0 + pix / TS) << 16) | (X0 + pix % TS),
+                             (dm << 8) | cov);
         }
         __syncwarp();
     }
@@ -902,7 +908,7 @@ __device__ __forceinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, ui
         if (valid && rank == r) {
 #pragma unroll
             for (int k = 0; k < S; ++k)
-                if ((dm >> k) & 1u) sm.cb[pix * S + k] = argb;
+                if ((dm >> k) & 1u) sm.cb[k * C::NPIX + pix] = argb;
         }
         __syncwarp();
     }
@@ -1079,9 +1085,19 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                     const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
                     const uint32_t nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
                     uint32_t s1 = lx0, e1 = lx1, s2 = lx0, e2 = lx1;
-                    if (nrows > 0 && lx1 - lx0 >= 4) {
-                        line_span<S, TS>(sm, it_l, 0u, first, X0, Y0, s1, e1);
-                        if (nrows > 1) line_span<S, TS>(sm, it_l, 0u, first + kRasterWarps, X0, Y0, s2, e2);
+                    if (lx1 - lx0 >= 4) {
+#pragma unroll 1
+                        for (uint32_t rw = 0; rw < nrows; ++rw) {
+                            uint32_t a0 = lx0, a1 = lx1;
+                            line_span<S, TS>(sm, it_l, 0u, first + rw * kRasterWarps, X0, Y0, a0, a1);
+                            if (rw == 0) {
+                                s1 = a0;
+                                e1 = a1;
+                            } else {
+                                s2 = a0;
+                                e2 = a1;
+                            }
+                        }
                     }
                     const uint32_t w1 = nrows > 0 ? e1 - s1 : 0u, w2 = nrows > 1 ? e2 - s2 : 0u;
                     c = w1 + w2;
@@ -1196,12 +1212,15 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
         const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
         if (x >= W || y >= H) continue;
         const unsigned long long o = (unsigned long long)y * W + x;
-        f.out[o] = box_filter<S>(&sm.cb[p * S]);
+        uint32_t smp[S];
+#pragma unroll
+        for (int q = 0; q < S; ++q) smp[q] = sm.cb[q * C::NPIX + p];
+        f.out[o] = box_filter<S>(smp);
         if (f.dbg_depth) {
 #pragma unroll
             for (int q = 0; q < S; ++q) {
-                f.dbg_depth[o * S + q] = sm.zb[p * S + q];
-                f.dbg_color[o * S + q] = sm.cb[p * S + q];
+                f.dbg_depth[o * S + q] = sm.zb[q * C::NPIX + p];
+                f.dbg_color[o * S + q] = sm.cb[q * C::NPIX + p];
             }
         }
     }
