@@ -49,11 +49,6 @@ int choose_tile(int w, int h, int msaa, int req) {
     return 0;
 }
 
-static uint32_t chunk_size_for(uint32_t ntris) {
-    uint32_t c = (ntris + 303u) / 304u;
-    c = (c + 255u) & ~255u;
-    return std::min<uint32_t>(std::max<uint32_t>(c, 512u), 8192u);
-}
 
 rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
     if (jobs.empty()) return RAST_OK;

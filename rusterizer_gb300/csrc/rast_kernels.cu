@@ -357,6 +357,9 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict_
 // ===================================================================== binning: scatter
 
 constexpr int kScatterThreads = 256;
+constexpr int kScatterWarps = kScatterThreads / 32;
+constexpr int kScatterTriPerThread = 2;
+constexpr int kScatterWindow = kScatterThreads * kScatterTriPerThread;  // triangles per batch
 constexpr int kPairsPerBatch = 512;  // (triangle, tile) pairs ranked per batch
 constexpr uint32_t kBigTri = 32;     // triangles over more tiles are binned alone, tile-parallel
 constexpr int kHashSlots = 1024;     // open-addressing table over tile ids, load <= 0.5
@@ -366,20 +369,26 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t t) {
     return (t * 2654435761u) >> (32 - 10);
 }
 
-// Ranks every (triangle, tile) pair of a chunk in submission order: per batch, a bit per
-// triangle per touched tile (hmask) gives each pair its rank among the batch's pairs of the
-// same tile; run_off carries each tile's running position across batches.
+// Bins the (triangle, tile) pairs of a chunk in submission order. Per batch of up to
+// kScatterWindow triangles (two consecutive ones per thread, so each warp holds a contiguous
+// run) and kPairsPerBatch pairs, every warp walks its pairs 32 at a time: lanes with the same
+// tile (match_any) take consecutive ranks from the warp's counter for that tile (wcnt, found
+// through a small hash of the batch's tiles). A pair's position is then the tile's running
+// offset + the counts of the earlier warps + its rank in its warp. A triangle over more than
+// kBigTri tiles ends a batch and is binned alone, tile-parallel.
 __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const ChunkDev* __restrict__ chunks, const DrawDev* __restrict__ draws,
     const FrameDev* __restrict__ frames, Scratch s) {
     extern __shared__ uint32_t run_off[];
     __shared__ uint32_t hkey[kHashSlots];
-    __shared__ uint32_t hmask[kHashSlots][kScatterThreads / 32];
+    __shared__ uint16_t wcnt[kHashSlots][kScatterWarps];
     __shared__ uint16_t slot_list[kPairsPerBatch];
-    __shared__ uint32_t nslots;
+    __shared__ uint16_t ptile[kPairsPerBatch], pslot[kPairsPerBatch], prank[kPairsPerBatch];
+    __shared__ uint16_t ptri[kPairsPerBatch];
+    __shared__ unsigned long long trect[kScatterWindow];
+    __shared__ uint32_t tclip[kScatterWindow / 32];
+    __shared__ uint32_t nslots, take_s;
     __shared__ uint32_t tmp[33];
-    __shared__ unsigned long long rect0;
-    __shared__ uint32_t aux0, n0s, big0;
     if (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) return;
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
@@ -391,88 +400,171 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     for (uint32_t h = threadIdx.x; h < (uint32_t)kHashSlots; h += blockDim.x) {
         hkey[h] = kHashEmpty;
 #pragma unroll
-        for (int w = 0; w < kScatterThreads / 32; ++w) hmask[h][w] = 0;
+        for (int w = 0; w < kScatterWarps; ++w) wcnt[h][w] = 0;
     }
     if (threadIdx.x == 0) nslots = 0;
     __syncthreads();
     uint32_t* bins = s.bins + f.bin_base;
     const unsigned long long cap = f.bin_cap;
     const uint32_t gbase = f.rect_base + d.tbase + ch.tri_begin;
+    const uint32_t fbase = d.tbase + ch.tri_begin;  // frame triangle index of the chunk's first
     const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
     uint32_t base = 0;
     while (base < ch.tri_count) {
-        const uint32_t i = base + threadIdx.x;
-        const bool live = i < ch.tri_count;
-        const unsigned long long rect = live ? s.tri_rect[gbase + i] : kRectEmpty;
-        const bool clipped = live && s.tri_aux[gbase + i] != kNone;
-        const uint32_t n = rect_tiles(rect, ts);
-        if (threadIdx.x == 0) {
-            big0 = kScatterThreads;
-            n0s = n;
-            rect0 = rect;
-            aux0 = clipped;
+        // ---- this thread's two triangles: pixel boxes, clipped flags, tile counts
+        unsigned long long r[kScatterTriPerThread];
+        uint32_t n[kScatterTriPerThread];
+        uint32_t mine = 0;
+#pragma unroll
+        for (int j = 0; j < kScatterTriPerThread; ++j) {
+            const uint32_t v = threadIdx.x * kScatterTriPerThread + j;
+            const uint32_t i = base + v;
+            const bool live = i < ch.tri_count;
+            r[j] = live ? s.tri_rect[gbase + i] : kRectEmpty;
+            const bool clipped = live && s.tri_aux[gbase + i] != kNone;
+            n[j] = rect_tiles(r[j], ts);
+            trect[v] = r[j];
+            const uint32_t cb = __ballot_sync(0xFFFFFFFFu, clipped);
+            // bit v of tclip: interleave the two ballots back into window order
+            if (lane == 0) {
+                uint32_t lo = 0, hi = 0;
+                for (int q = 0; q < 16; ++q) {
+                    lo |= ((cb >> q) & 1u) << (2 * q + j);
+                    hi |= ((cb >> (q + 16)) & 1u) << (2 * q + j);
+                }
+                if (j == 0) {
+                    tclip[warp * 2] = lo;
+                    tclip[warp * 2 + 1] = hi;
+                } else {
+                    tclip[warp * 2] |= lo;
+                    tclip[warp * 2 + 1] |= hi;
+                }
+            }
+            mine += n[j];
         }
+        if (threadIdx.x == 0) take_s = kScatterWindow;
         uint32_t total;
-        const uint32_t excl = block_excl_scan(n, tmp, total);  // its barriers order big0
-        if (n > kBigTri) atomicMin(&big0, threadIdx.x);
+        const uint32_t excl = block_excl_scan(mine, tmp, total);  // its barriers order take_s
+        // the batch: a prefix of the window within the pair budget
+        {
+            uint32_t run = excl;
+#pragma unroll
+            for (int j = 0; j < kScatterTriPerThread; ++j) {
+                const uint32_t v = threadIdx.x * kScatterTriPerThread + j;
+                run += n[j];
+                if (run > (uint32_t)kPairsPerBatch || n[j] > kBigTri) {
+                    atomicMin(&take_s, v);
+                    break;
+                }
+            }
+        }
         __syncthreads();
-        const uint32_t n0 = n0s;
-        const unsigned long long r0 = rect0;
-        const bool c0 = aux0 != 0;
-        const uint32_t firstbig = big0;
-        __syncthreads();
-        const uint32_t frame_tri = d.tbase + ch.tri_begin + i;  // bin entry: triangle in frame
-        if (firstbig == 0) {
-            // a single large triangle: its tiles are distinct, each takes the next position
-            const uint32_t g0 = d.tbase + ch.tri_begin + base;
+        uint32_t take = take_s;
+        if (take == 0) {
+            // a single triangle over more than kBigTri tiles: its tiles are distinct, each
+            // takes the next position
+            const unsigned long long r0 = trect[0];
+            const bool c0 = tclip[0] & 1u;
             uint32_t x0, y0, x1, y1;
             tile_rect(r0, ts, x0, y0, x1, y1);
-            const uint32_t w = x1 - x0 + 1;
+            const uint32_t w = x1 - x0 + 1, n0 = rect_tiles(r0, ts);
             for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
                 const uint32_t ttx = x0 + k % w, tty = y0 + k / w;
                 const uint32_t t = tty * tx + ttx;
                 const uint32_t pos = run_off[t];
-                if (pos < cap) bins[pos] = bin_entry(g0, c0, r0, ttx, tty, ts);
+                if (pos < cap) bins[pos] = bin_entry(fbase + base, c0, r0, ttx, tty, ts);
                 run_off[t] = pos + 1;
             }
             __syncthreads();
             base += 1;
             continue;
         }
-        // a prefix of small triangles: stop at the first large one and at the pair budget
-        const bool part = live && threadIdx.x < firstbig && (excl + n <= (uint32_t)kPairsPerBatch);
-        const uint32_t take = __syncthreads_count(part);
-        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-        if (part && n) tile_rect(rect, ts, x0, y0, x1, y1);
-        if (part && n) {
-            for (uint32_t y = y0; y <= y1; ++y)
-                for (uint32_t x = x0; x <= x1; ++x) {
-                    const uint32_t t = y * tx + x;
-                    uint32_t h = hash_slot(t);
-                    while (true) {
-                        const uint32_t old = atomicCAS(&hkey[h], kHashEmpty, t);
-                        if (old == kHashEmpty) {
-                            slot_list[atomicAdd(&nslots, 1u)] = (uint16_t)h;
-                            break;
-                        }
-                        if (old == t) break;
-                        h = (h + 1) & (kHashSlots - 1);
+        take = min(take, ch.tri_count - base);
+        // ---- per warp, its pairs in order, 32 at a time: rank within the warp per tile
+        uint32_t pc = 0;  // this thread's pairs in the batch
+#pragma unroll
+        for (int j = 0; j < kScatterTriPerThread; ++j)
+            if (threadIdx.x * kScatterTriPerThread + j < take) pc += n[j];
+        uint32_t winc = pc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, winc, o);
+            if (lane >= (uint32_t)o) winc += y;
+        }
+        const uint32_t wtotal = __shfl_sync(0xFFFFFFFFu, winc, 31);
+        const uint32_t wbase = __shfl_sync(0xFFFFFFFFu, excl, 0);  // block index of the warp's first pair
+        for (uint32_t rb = 0; rb < wtotal; rb += 32) {
+            const uint32_t pi = rb + lane;
+            uint32_t sl = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const uint32_t v = __shfl_sync(0xFFFFFFFFu, winc, sl + st - 1);
+                if (v <= pi) sl += st;
+            }
+            const uint32_t src = min(sl, 31u);
+            const uint32_t o = pi - __shfl_sync(0xFFFFFFFFu, winc - pc, src);
+            const uint32_t n0 = __shfl_sync(0xFFFFFFFFu, n[0], src);
+            uint32_t key = 0xFFFFFFFFu - lane, v = 0;
+            if (pi < wtotal) {
+                const uint32_t j = o < n0 ? 0u : 1u, k = o < n0 ? o : o - n0;
+                v = (warp * 32 + src) * kScatterTriPerThread + j;
+                uint32_t x0, y0, x1, y1;
+                tile_rect(trect[v], ts, x0, y0, x1, y1);
+                const uint32_t w = x1 - x0 + 1;
+                const uint32_t ky = k < w ? 0u : k / w;
+                key = (y0 + ky) * tx + x0 + (k - ky * w);
+            }
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+            const uint32_t leader = __ffs(peers) - 1;
+            uint32_t slot = 0, old = 0;
+            if (pi < wtotal && lane == leader) {
+                uint32_t h = hash_slot(key);
+                while (true) {
+                    const uint32_t prev = atomicCAS(&hkey[h], kHashEmpty, key);
+                    if (prev == kHashEmpty) {
+                        slot_list[atomicAdd(&nslots, 1u)] = (uint16_t)h;
+                        break;
                     }
-                    atomicOr(&hmask[h][warp], 1u << lane);
+                    if (prev == key) break;
+                    h = (h + 1) & (kHashSlots - 1);
                 }
+                slot = h;
+                old = wcnt[h][warp];
+                wcnt[h][warp] = (uint16_t)(old + __popc(peers));
+            }
+            slot = __shfl_sync(0xFFFFFFFFu, slot, leader);
+            old = __shfl_sync(0xFFFFFFFFu, old, leader);
+            if (pi < wtotal) {
+                const uint32_t bp = wbase + pi;
+                ptile[bp] = (uint16_t)key;
+                pslot[bp] = (uint16_t)slot;
+                prank[bp] = (uint16_t)(old + __popc(peers & lanemask_lt()));
+                ptri[bp] = (uint16_t)v;
+            }
         }
         __syncthreads();
-        if (part && n) {
-            for (uint32_t y = y0; y <= y1; ++y)
-                for (uint32_t x = x0; x <= x1; ++x) {
-                    const uint32_t t = y * tx + x;
-                    uint32_t h = hash_slot(t);
-                    while (hkey[h] != t) h = (h + 1) & (kHashSlots - 1);
-                    uint32_t before = __popc(hmask[h][warp] & lanemask_lt());
-                    for (uint32_t w2 = 0; w2 < warp; ++w2) before += __popc(hmask[h][w2]);
-                    const uint32_t pos = run_off[t] + before;
-                    if (pos < cap) bins[pos] = bin_entry(frame_tri, clipped, rect, x, y, ts);
-                }
+        // ---- positions: running offset + earlier warps' counts + rank in the warp
+        uint32_t npairs = 0;  // pairs of the batch: those of the taken triangles
+        {
+            const uint32_t t_last = take - 1;  // its thread holds the end of the batch's pairs
+            if (threadIdx.x == t_last / kScatterTriPerThread) {
+                uint32_t e = excl;
+#pragma unroll
+                for (int j = 0; j < kScatterTriPerThread; ++j)
+                    if (threadIdx.x * kScatterTriPerThread + j < take) e += n[j];
+                tmp[0] = e;
+            }
+        }
+        __syncthreads();
+        npairs = tmp[0];
+        for (uint32_t bp = threadIdx.x; bp < npairs; bp += blockDim.x) {
+            const uint32_t t = ptile[bp], slot = pslot[bp], v = ptri[bp];
+            const uint32_t pw = v / (32 * kScatterTriPerThread);
+            uint32_t before = prank[bp];
+            for (uint32_t w2 = 0; w2 < pw; ++w2) before += wcnt[slot][w2];
+            const uint32_t pos = run_off[t] + before;
+            const bool clipped = (tclip[v >> 5] >> (v & 31u)) & 1u;
+            if (pos < cap) bins[pos] = bin_entry(fbase + base + v, clipped, trect[v], t % tx, t / tx, ts);
         }
         __syncthreads();
         const uint32_t ns = nslots;
@@ -480,9 +572,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             const uint32_t h = slot_list[j];
             uint32_t cnt = 0;
 #pragma unroll
-            for (int w2 = 0; w2 < kScatterThreads / 32; ++w2) {
-                cnt += __popc(hmask[h][w2]);
-                hmask[h][w2] = 0;
+            for (int w2 = 0; w2 < kScatterWarps; ++w2) {
+                cnt += wcnt[h][w2];
+                wcnt[h][w2] = 0;
             }
             run_off[hkey[h]] += cnt;
             hkey[h] = kHashEmpty;

@@ -96,9 +96,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // descriptors, built on the stack
-    uint32_t cs = (ntris + 303u) / 304u;
-    cs = (cs + 255u) & ~255u;
-    cs = cs < 512u ? 512u : (cs > 8192u ? 8192u : cs);
+    const uint32_t cs = chunk_size_for(ntris);
     const uint32_t nchunks = (ntris + cs - 1) / cs;
     const uint32_t nvb = (nverts + 255u) / 256u;
     FrameDev F{};

@@ -55,8 +55,7 @@ using ShapeKey = std::tuple<uint32_t, int, int, int, int>;  // mesh, width, heig
 uint64_t footprint_of(const rast_ctx* c, const rast_scene& s, int ts, uint64_t bins) {
     const MeshRec& m = c->meshes[s.mesh];
     const uint64_t tiles = (uint64_t)((s.width + ts - 1) / ts) * ((s.height + ts - 1) / ts);
-    uint64_t cs = (m.ntris + 303u) / 304u;
-    cs = std::min<uint64_t>(std::max<uint64_t>((cs + 255u) & ~255ull, 512u), 8192u);
+    const uint64_t cs = chunk_size_for(m.ntris);
     const uint64_t chunks = (m.ntris + cs - 1) / cs;
     const uint64_t bin_cap = std::max<uint64_t>(bins, 4ull * m.ntris + tiles + 1024ull);
     const uint64_t split = raster_edge(ts) < ts ? 16ull * (bin_cap + tiles) : 0ull;
