@@ -628,7 +628,6 @@ struct RasterSmem {
     uint8_t sdm[kRasterWarps][C::QC];
     float inv255[256];
     int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
-    uint32_t own[kRasterWarps + 1];  // column mode: warp w owns columns [own[w], own[w+1])
     uint32_t tmp[40];
     uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split mode
 
@@ -792,15 +791,15 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
     }
 }
 
-// Chooses how the tile's pixels are divided among the warps for one batch, by candidate-pixel
-// work: either interleaved rows (row r to warp r % kRasterWarps; suits scattered triangles) or
-// kRasterWarps contiguous column ranges of about equal work (suits runs of small triangles
-// along a screen row, which crowd into a few rows). Each warp then owns its pixels for the
-// batch, which keeps every pixel's fragments in one warp and in submission order. mode 0 =
-// rows, 1 = columns, own[] = the column range bounds. Called by one warp.
+// Chooses how the tile's pixels are divided among the warps for one batch: interleaved rows
+// (row r to warp r % kRasterWarps; suits scattered triangles) or interleaved columns (suits
+// runs of small triangles along a screen row, which crowd into a few rows), whichever gives
+// the lighter heaviest warp by candidate-pixel work. Either way each warp owns its pixels for
+// the batch, which keeps every pixel's fragments in one warp and in submission order, and an
+// item meets each warp on at most TS / kRasterWarps lines. Returns 0 for rows, 1 for columns.
+// Called by one warp.
 template <int TS>
-__device__ __forceinline__ void split_work(const int* rowd, const int* cold, uint32_t* own,
-                                           uint32_t* mode_out) {
+__device__ __forceinline__ uint32_t split_work(const int* rowd, const int* cold) {
     const uint32_t lane = lane_id();
     // per-line work from the difference arrays
     int rw = lane < (uint32_t)TS ? rowd[lane] : 0, cw = lane < (uint32_t)TS ? cold[lane] : 0;
@@ -814,34 +813,14 @@ __device__ __forceinline__ void split_work(const int* rowd, const int* cold, uin
     }
     const uint32_t wr = lane < (uint32_t)TS ? (uint32_t)rw : 0u;
     const uint32_t wc = lane < (uint32_t)TS ? (uint32_t)cw : 0u;
-    // interleaved rows
-    uint32_t mrow = 0;
+    uint32_t mrow = 0, mcol = 0;
 #pragma unroll
-    for (int k = 0; k < kRasterWarps; ++k)
-        mrow = max(mrow, __reduce_add_sync(0xFFFFFFFFu, (lane % kRasterWarps) == (uint32_t)k ? wr : 0u));
-    // contiguous column ranges: a column goes to the range that holds the midpoint of its work
-    uint32_t incl = wc;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
+    for (int k = 0; k < kRasterWarps; ++k) {
+        const bool mine = (lane % kRasterWarps) == (uint32_t)k;
+        mrow = max(mrow, __reduce_add_sync(0xFFFFFFFFu, mine ? wr : 0u));
+        mcol = max(mcol, __reduce_add_sync(0xFFFFFFFFu, mine ? wc : 0u));
     }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    const uint32_t excl = incl - wc;
-    uint32_t part;
-    if (lane >= (uint32_t)TS) part = kRasterWarps;
-    else if (total == 0) part = lane * kRasterWarps / TS;
-    else part = min((uint32_t)(kRasterWarps - 1), ((2u * excl + wc) * kRasterWarps) / (2u * total));
-    uint32_t mcol = 0;
-#pragma unroll
-    for (int k = 0; k < kRasterWarps; ++k)
-        mcol = max(mcol, __reduce_add_sync(0xFFFFFFFFu, part == (uint32_t)k ? wc : 0u));
-#pragma unroll
-    for (int k = 0; k <= kRasterWarps; ++k) {
-        const uint32_t bnd = __popc(__ballot_sync(0xFFFFFFFFu, part < (uint32_t)k));
-        if (lane == 0) own[k] = bnd;
-    }
-    if (lane == 0) *mode_out = mcol < mrow ? 1u : 0u;
+    return mcol < mrow ? 1u : 0u;
 }
 
 // Appends one fragment record to the debug log (rast_debug_log_enable); kept out of line.
@@ -1113,7 +1092,10 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             if (take < window) break;  // the batch is full
         }
         // ---- B. divide the tile's pixels among the warps; which warps each item reaches
-        if (warp == 0) split_work<TS>(sm.rowd, sm.cold, sm.own, &sm.misc[5]);
+        if (warp == 0) {
+            const uint32_t m = split_work<TS>(sm.rowd, sm.cold);
+            if (lane == 0) sm.misc[5] = m;
+        }
         __syncthreads();
         const uint32_t mode = sm.misc[5];
         {
@@ -1121,23 +1103,14 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             uint32_t wm = 0;
             if (t < nit) {
                 const uint32_t r = sm.irect[t];
-                if (mode == 0) {
-                    // interleaved rows: warps of rows ly0 .. ly1 - 1
-                    const uint32_t ly0 = (r >> 8) & 0xFFu, ly1 = r >> 24;
-                    if (ly1 > ly0) {
-                        const uint32_t nrow = ly1 - ly0;
-                        wm = nrow >= (uint32_t)kRasterWarps
-                                 ? (1u << kRasterWarps) - 1u
-                                 : (((1u << nrow) - 1u) << (ly0 % kRasterWarps));
-                        wm = (wm | (wm >> kRasterWarps)) & ((1u << kRasterWarps) - 1u);
-                    }
-                } else {
-                    const uint32_t a0 = r & 0xFFu, a1 = (r >> 16) & 0xFFu;
-                    if (a1 > a0) {
-#pragma unroll
-                        for (int w = 0; w < kRasterWarps; ++w)
-                            if (a0 < sm.own[w + 1] && a1 > sm.own[w]) wm |= 1u << w;
-                    }
+                // the warps of lines a0 .. a1 - 1 (rows, or columns in column mode)
+                const uint32_t a0 = mode ? (r & 0xFFu) : ((r >> 8) & 0xFFu);
+                const uint32_t a1 = mode ? ((r >> 16) & 0xFFu) : (r >> 24);
+                if (a1 > a0) {
+                    const uint32_t nl = a1 - a0;
+                    wm = nl >= (uint32_t)kRasterWarps ? (1u << kRasterWarps) - 1u
+                                                      : (((1u << nl) - 1u) << (a0 % kRasterWarps));
+                    wm = (wm | (wm >> kRasterWarps)) & ((1u << kRasterWarps) - 1u);
                 }
             }
 #pragma unroll
@@ -1147,12 +1120,11 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             }
         }
         __syncthreads();
-        // ---- C. per warp, in submission order: the candidate pixels of its items inside its
-        // range (in row mode each of an item's rows trimmed to the pixels that can hold a
-        // covered sample, line_span); coverage (EdgeFunctions::eval, mod.rs:134-146) and
+        // ---- C. per warp, in submission order: the candidate pixels of its items on its
+        // lines (each line trimmed to the pixels that can hold a covered sample, line_span);
+        // coverage (EdgeFunctions::eval, mod.rs:134-146) and
         // sample depths (RasterizerTriangle::fragment, mod.rs:225-253) of each; then ordered
         // depth test and shading of the covered fragments
-        const uint32_t olo = sm.own[warp], ohi = sm.own[warp + 1];
         uint32_t nmine = 0;
 #pragma unroll
         for (int src = 0; src < C::IC / 32; ++src) {
@@ -1165,41 +1137,36 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
         for (uint32_t gb = 0; gb < nmine; gb += 32) {
             const bool act = gb + lane < nmine;
             const uint32_t it_l = act ? sm.wlist[warp][gb + lane] : 0u;
-            // candidates of the lane's item and where they lie:
-            //   row mode:    first row | first-row start << 5 | first-row length << 10 |
-            //                second-row start << 15 (second row = first + kRasterWarps)
-            //   column mode: x0 | y0 << 5 | width << 10 | ceil(65536 / width) << 15
+            // candidates of the lane's item: its lines owned by this warp (rows, or columns in
+            // column mode: the first, then first + kRasterWarps), each trimmed by line_span;
+            // geo = first line | first-line start << 5 | first-line length << 10 |
+            // second-line start << 15
             uint32_t c = 0, geo = 0;
             if (act) {
                 const uint32_t r = sm.irect[it_l];
                 const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
-                if (mode == 0) {
-                    const uint32_t first = ly0 + ((warp + kRasterWarps - (ly0 % kRasterWarps)) % kRasterWarps);
-                    const uint32_t nrows = first < ly1 ? (ly1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
-                    uint32_t s1 = lx0, e1 = lx1, s2 = lx0, e2 = lx1;
-                    if (lx1 - lx0 >= 4) {
+                const uint32_t l0 = mode ? lx0 : ly0, l1 = mode ? lx1 : ly1;  // lines
+                const uint32_t b0 = mode ? ly0 : lx0, b1 = mode ? ly1 : lx1;  // along each line
+                const uint32_t first = l0 + ((warp + kRasterWarps - (l0 % kRasterWarps)) % kRasterWarps);
+                const uint32_t nlines = first < l1 ? (l1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
+                uint32_t s1 = b0, e1 = b1, s2 = b0, e2 = b1;
+                // lines shorter than 4 pixels are cheaper to test whole than to trim
+                const uint32_t ntrim = b1 - b0 >= 4 ? nlines : 0u;
 #pragma unroll 1
-                        for (uint32_t rw = 0; rw < nrows; ++rw) {
-                            uint32_t a0 = lx0, a1 = lx1;
-                            line_span<S, TS>(sm, it_l, 0u, first + rw * kRasterWarps, X0, Y0, a0, a1);
-                            if (rw == 0) {
-                                s1 = a0;
-                                e1 = a1;
-                            } else {
-                                s2 = a0;
-                                e2 = a1;
-                            }
-                        }
+                for (uint32_t ln = 0; ln < ntrim; ++ln) {
+                    uint32_t a0 = b0, a1 = b1;
+                    line_span<S, TS>(sm, it_l, mode, first + ln * kRasterWarps, X0, Y0, a0, a1);
+                    if (ln == 0) {
+                        s1 = a0;
+                        e1 = a1;
+                    } else {
+                        s2 = a0;
+                        e2 = a1;
                     }
-                    const uint32_t w1 = nrows > 0 ? e1 - s1 : 0u, w2 = nrows > 1 ? e2 - s2 : 0u;
-                    c = w1 + w2;
-                    geo = first | (s1 << 5) | (w1 << 10) | (s2 << 15);
-                } else {
-                    const uint32_t cx0 = max(lx0, olo), cx1 = min(lx1, ohi);
-                    const uint32_t sw = cx1 > cx0 ? cx1 - cx0 : 1u;
-                    c = cx1 > cx0 ? sw * (ly1 - ly0) : 0u;
-                    geo = cx0 | (ly0 << 5) | (sw << 10) | (((65535u + sw) / sw) << 15);
                 }
+                const uint32_t w1 = nlines > 0 ? e1 - s1 : 0u, w2 = nlines > 1 ? e2 - s2 : 0u;
+                c = w1 + w2;
+                geo = first | (s1 << 5) | (w1 << 10) | (s2 << 15);
             }
             uint32_t incl = c;
 #pragma unroll
@@ -1227,18 +1194,11 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 for (int k = 0; k < S; ++k) z[k] = 0.0f;
                 if (p < total) {
                     const uint32_t rr = p - exc;
-                    uint32_t lx, ly;
-                    if (mode == 0) {
-                        const uint32_t w1 = (gg >> 10) & 31u;
-                        const bool second = rr >= w1;
-                        lx = second ? ((gg >> 15) & 31u) + (rr - w1) : ((gg >> 5) & 31u) + rr;
-                        ly = (gg & 31u) + (second ? (uint32_t)kRasterWarps : 0u);
-                    } else {
-                        // rr / width by multiply-shift: exact while rr * width < 65536 (rr < 256)
-                        const uint32_t sw = (gg >> 10) & 31u, q = (rr * (gg >> 15)) >> 16;
-                        lx = (gg & 31u) + rr - q * sw;
-                        ly = ((gg >> 5) & 31u) + q;
-                    }
+                    const uint32_t w1 = (gg >> 10) & 31u;
+                    const bool second = rr >= w1;
+                    const uint32_t along = second ? ((gg >> 15) & 31u) + (rr - w1) : ((gg >> 5) & 31u) + rr;
+                    const uint32_t line = (gg & 31u) + (second ? (uint32_t)kRasterWarps : 0u);
+                    const uint32_t lx = mode ? line : along, ly = mode ? along : line;
                     pix = ly * TS + lx;
                     const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
                     float n0x, n0y, n1x, n1y, n2x, n2y;
