@@ -395,8 +395,10 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const FrameDev& f = frames[d.frame];
     const uint32_t nt = f.ntiles, tx = f.tiles_x, ts = (uint32_t)f.ts;
     const uint32_t* crow = s.counts + f.count_base + (unsigned long long)ch.row * nt;
-    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x)
-        run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
+    // run_off[t]: the chunk's next position in tile t, loaded when the chunk first meets t
+    // (a chunk of small triangles meets few of the frame's tiles); valid: one bit per tile
+    uint32_t* valid = run_off + nt;
+    for (uint32_t t = threadIdx.x; t < (nt + 31u) / 32u; t += blockDim.x) valid[t] = 0;
     for (uint32_t h = threadIdx.x; h < (uint32_t)kHashSlots; h += blockDim.x) {
         hkey[h] = kHashEmpty;
 #pragma unroll
@@ -471,6 +473,10 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
                 const uint32_t ttx = x0 + k % w, tty = y0 + k / w;
                 const uint32_t t = tty * tx + ttx;
+                if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
+                    run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
+                    atomicOr(&valid[t >> 5], 1u << (t & 31u));
+                }
                 const uint32_t pos = run_off[t];
                 if (pos < cap) bins[pos] = bin_entry(fbase + base, c0, r0, ttx, tty, ts);
                 run_off[t] = pos + 1;
@@ -544,6 +550,14 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         }
         __syncthreads();
         // ---- positions: running offset + earlier warps' counts + rank in the warp
+        // first meeting of a tile in this chunk: load its running offset
+        for (uint32_t j = threadIdx.x; j < nslots; j += blockDim.x) {
+            const uint32_t t = hkey[slot_list[j]];
+            if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
+                run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
+                atomicOr(&valid[t >> 5], 1u << (t & 31u));
+            }
+        }
         uint32_t npairs = 0;  // pairs of the batch: those of the taken triangles
         {
             const uint32_t t_last = take - 1;  // its thread holds the end of the batch's pairs
@@ -1458,12 +1472,13 @@ cudaError_t launch_bin_scatter(const LaunchArgs& a) {
     if (a.nchunks == 0) return cudaSuccess;
     static int configured = 0;
     const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
-    if (bytes > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    const int need = bytes + (int)(((a.max_tiles + 31) / 32) * sizeof(uint32_t));
+    if (need > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
         if (e != cudaSuccess) return e;
-        configured = bytes;
+        configured = need;
     }
-    k_bin_scatter<<<a.nchunks, kScatterThreads, bytes, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
+    k_bin_scatter<<<a.nchunks, kScatterThreads, need, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
     return cudaGetLastError();
 }
 
