@@ -150,7 +150,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                   E.tri_rect.reserve(ttot) && E.tri_aux.reserve(ttot) &&
                   E.counts.reserve(count_tot) && E.tile_start.reserve(tile_tot) &&
                   E.tile_count.reserve(tile_tot) && E.tile_order.reserve(tile_tot) &&
-                  E.bins.reserve(bin_tot) && E.qbins.reserve(qbin_tot) &&
+                  E.bins.reserve(bin_tot) && E.qbins.reserve(qbin_tot) && E.clip_list.reserve(3ull * ttot) &&
                   E.qcount.reserve(qbin_tot ? 4ull * tile_tot : 0ull) &&
                   E.clip_store.reserve(std::max<uint64_t>(clip_est, E.clip_hint)) &&
                   E.frame_need.reserve(frames.size());
@@ -215,6 +215,9 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         S.clip_store = E.clip_store.p;
         S.clip_cap = E.clip_store.cap;
         S.clip_used = &E.d_state->clip_used;
+        S.clip_list = E.clip_list.p;
+        S.clip_list_cap = ttot;
+        S.clip_n = &E.d_state->clip_n;
         S.status = &E.d_state->status;
         S.stats = E.d_state->stats;
         S.frame_need = E.frame_need.p;

@@ -125,10 +125,6 @@ __device__ __forceinline__ int clip_classify(float area, uint32_t c0, uint32_t c
     return 2;
 }
 
-// Sutherland-Hodgman stage of try_clip (src/rasterizer/clipping.rs:117-177) against the six
-// planes in order. Returns the polygon size (0 = Outside); -1 if it would exceed kMaxPoly.
-__device__ __noinline__ int clip_polygon(const ClipVert in[3], ClipVert* poly /* kMaxPoly */);
-
 // ------------------------------------------------------------------ triangle setup
 
 // RasterizerTriangle (src/rasterizer/mod.rs:177-222): edge points, inward normals, screen

@@ -174,6 +174,8 @@ struct DeviceState {
     unsigned long long stats[STAT_COUNT];
     unsigned long long clip_used;
     unsigned long long log_n;
+    unsigned int clip_n;     // triangles queued for the warp clipper
+    unsigned int pad2;
     unsigned int queue[32];  // raster tile queues, 4 counters per (msaa, tile) group
 };
 
@@ -182,7 +184,7 @@ struct Engine {
     DevBuf<float4> vclip, vscr;
     DevBuf<uint16_t> vcode;
     DevBuf<unsigned long long> tri_rect;
-    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, tile_order, bins, qbins, qcount;
+    DevBuf<uint32_t> tri_aux, counts, tile_start, tile_count, tile_order, bins, qbins, qcount, clip_list;
     DevBuf<float> clip_store;
     DevBuf<unsigned long long> frame_need;
     DevBuf<uint32_t> log;

@@ -20,43 +20,6 @@
 
 namespace rast {
 
-// ===================================================================== Sutherland-Hodgman
-
-__device__ __noinline__ int clip_polygon(const ClipVert in[3], ClipVert* poly) {
-    ClipVert buf[kMaxPoly];
-    ClipVert* cur = poly;
-    ClipVert* nxt = buf;
-    int cn = 3;
-    for (int k = 0; k < 3; ++k) cur[k] = in[k];
-    for (int plane = 0; plane < 6; ++plane) {
-        int on = 0;
-        for (int i = 0; i < cn; ++i) {
-            int pi = (i + cn - 1) % cn;
-            float dp = distance_measure(plane, cur[pi].p);
-            float dc = distance_measure(plane, cur[i].p);
-            bool pin = dp >= 0.0f, cin = dc >= 0.0f;
-            int need = (pin && cin) ? 1 : (pin && !cin) ? 1 : (!pin && cin) ? 2 : 0;
-            if (on + need > kMaxPoly) return -1;
-            if (pin && cin) {
-                nxt[on++] = cur[i];
-            } else if (pin && !cin) {
-                clip_intersect(cur[pi], dp, cur[i], dc, nxt[on++]);
-            } else if (!pin && cin) {
-                clip_intersect(cur[pi], dp, cur[i], dc, nxt[on++]);
-                nxt[on++] = cur[i];
-            }
-        }
-        ClipVert* t = cur;
-        cur = nxt;
-        nxt = t;
-        cn = on;
-        if (cn == 0) break;
-    }
-    if (cn > 0 && cur != poly)
-        for (int k = 0; k < cn; ++k) poly[k] = cur[k];
-    return cn;
-}
-
 // ===================================================================== helpers
 
 __device__ __forceinline__ unsigned long long pack_rect(uint32_t x0, uint32_t y0, uint32_t x1,
@@ -167,7 +130,7 @@ __global__ void __launch_bounds__(256) k_vertex(const DrawDev* __restrict__ draw
 // try_clip + divide + viewport + bounding box for one triangle (src/rasterizer/mod.rs:425-441).
 // Returns its pixel box (kRectEmpty when nothing can be covered) and, for a clipped
 // triangle, the offset of its polygon in the clip store.
-__device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t tri,
+__device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t di, uint32_t tri, uint32_t row,
                                   const Scratch& s, unsigned long long& rect, uint32_t& aux) {
     rect = kRectEmpty;
     aux = kNone;
@@ -190,63 +153,177 @@ __device__ void classify_triangle(const DrawDev& d, const FrameDev& f, uint32_t 
         pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
         if (bx0 >= bx1 || by0 >= by1) return;
     } else {
-        ClipVert in[3];
-        const float4 cc[3] = {c0, c1, c2};
-        const uint32_t ii[3] = {i0, i1, i2};
-        for (int k = 0; k < 3; ++k) {
-            in[k].p[0] = cc[k].x;
-            in[k].p[1] = cc[k].y;
-            in[k].p[2] = cc[k].z;
-            in[k].p[3] = cc[k].w;
-            if (d.rgba) {
-                for (int q = 0; q < 4; ++q) in[k].a[q] = __ldg(d.rgba + 4ull * ii[k] + q);
-            } else {
-                for (int q = 0; q < 4; ++q) in[k].a[q] = 0.0f;
-            }
-            in[k].a[4] = __ldg(d.uv + 2ull * ii[k]);
-            in[k].a[5] = __ldg(d.uv + 2ull * ii[k] + 1);
-        }
-        ClipVert poly[kMaxPoly];
-        const int n = clip_polygon(in, poly);
-        if (n < 0) {
-            atomicOr(s.status, ST_CLIP_OVERFLOW);
-            return;
-        }
-        if (n < 3) return;
-        const unsigned long long need = 1ull + 10ull * (unsigned long long)n;
-        const unsigned long long off = atomicAdd(s.clip_used, need);
-        if (off + need > s.clip_cap) {
+        // straddles a clip plane: queued for k_clip, which clips it with one warp and adds its
+        // tiles to this chunk's counts
+        const uint32_t slot = atomicAdd(s.clip_n, 1u);
+        if (slot < s.clip_list_cap) {
+            uint32_t* L = s.clip_list + 3ull * slot;
+            L[0] = di;
+            L[1] = tri;
+            L[2] = row;
+        } else {
             atomicOr(s.status, ST_CLIP_STORE_OVERFLOW);
-            return;
         }
-        float* st = s.clip_store + off;
-        st[0] = __int_as_float(n);
-        float4 sc[kMaxPoly];
-        for (int k = 0; k < n; ++k) {
-            float4 cp = make_float4(poly[k].p[0], poly[k].p[1], poly[k].p[2], poly[k].p[3]);
-            sc[k] = to_screen(cp, (float)f.width, (float)f.height);
-            float* o = st + 1 + 10 * k;
-            o[0] = sc[k].x;
-            o[1] = sc[k].y;
-            o[2] = sc[k].z;
-            o[3] = sc[k].w;
-            for (int q = 0; q < 6; ++q) o[4 + q] = poly[k].a[q];
-        }
-        // fan [v0, v(i+1), v(i+2)] (src/rasterizer/clipping.rs:185-190): union of the pixel boxes
-        for (int t = 0; t + 2 < n; ++t) {
-            const float4 tv[3] = {sc[0], sc[t + 1], sc[t + 2]};
-            uint32_t a0, a1, b0, b1;
-            pixel_bbox(tv, f.width, f.height, a0, a1, b0, b1);
-            if (a0 >= a1 || b0 >= b1) continue;
-            bx0 = min(bx0, a0);
-            bx1 = max(bx1, a1);
-            by0 = min(by0, b0);
-            by1 = max(by1, b1);
-        }
-        aux = (uint32_t)off;
-        if (bx0 >= bx1 || by0 >= by1) return;
+        return;
     }
     rect = pack_rect(bx0, by0, bx1 - 1, by1 - 1);
+}
+
+// Sutherland-Hodgman against the six clip planes in CLIP_PLANES order
+// (src/rasterizer/clipping.rs:113-177) with the polygon spread over a warp: lane i holds
+// vertex i. Per plane every lane looks at its edge (previous vertex -> its vertex) and emits
+// nothing, the intersection, its vertex, or both, in the reference's order; an exclusive scan
+// of the emit counts places them. A plane every vertex is inside leaves the polygon as it is.
+// Returns the new vertex count, or -1 past 32 vertices. Called by a whole warp.
+__device__ __forceinline__ int warp_clip(ClipVert& v, int cn) {
+    const uint32_t lane = lane_id();
+    for (int plane = 0; plane < 6; ++plane) {
+        const bool live = lane < (uint32_t)cn;
+        const float dc = live ? distance_measure(plane, v.p) : 0.0f;
+        const bool cin = dc >= 0.0f;
+        if (__all_sync(0xFFFFFFFFu, !live || cin)) continue;
+        const uint32_t prev = live ? (lane + (uint32_t)cn - 1u) % (uint32_t)cn : lane;
+        ClipVert pv;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) pv.p[k] = __shfl_sync(0xFFFFFFFFu, v.p[k], prev);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) pv.a[k] = __shfl_sync(0xFFFFFFFFu, v.a[k], prev);
+        const float dp = __shfl_sync(0xFFFFFFFFu, dc, prev);
+        const bool pin = dp >= 0.0f;
+        uint32_t emit = 0;
+        if (live) emit = (pin && cin) ? 1u : (pin && !cin) ? 1u : (!pin && cin) ? 2u : 0u;
+        ClipVert first = v;  // both inside: the vertex itself
+        if (live && pin != cin) clip_intersect(pv, dp, v, dc, first);
+        uint32_t incl = emit;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (total > (uint32_t)kMaxPoly) return -1;
+        // new vertex `lane`: emitted by the lane whose inclusive count first exceeds it
+        uint32_t src = 0;
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1) {
+            const uint32_t c = __shfl_sync(0xFFFFFFFFu, incl, src + st - 1);
+            if (c <= lane) src += st;
+        }
+        src = min(src, 31u);
+        const uint32_t second = lane - (__shfl_sync(0xFFFFFFFFu, incl, src) - __shfl_sync(0xFFFFFFFFu, emit, src));
+        ClipVert nv;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float a = __shfl_sync(0xFFFFFFFFu, first.p[k], src), b = __shfl_sync(0xFFFFFFFFu, v.p[k], src);
+            nv.p[k] = second ? b : a;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float a = __shfl_sync(0xFFFFFFFFu, first.a[k], src), b = __shfl_sync(0xFFFFFFFFu, v.a[k], src);
+            nv.a[k] = second ? b : a;
+        }
+        v = nv;
+        cn = (int)total;
+        if (cn == 0) break;
+    }
+    return cn;
+}
+
+// Clips the queued straddling triangles, one warp per triangle: the polygon goes to the clip
+// store in screen space (to_screen per vertex, as the reference divides and maps the fan's
+// triangles, src/rasterizer/mod.rs:425-441), the union of the fan's pixel boxes
+// (clipping.rs:185-190) becomes the triangle's box, and its tiles are added to its chunk's
+// counts. Grid-stride over the queue.
+__global__ void __launch_bounds__(256) k_clip(const DrawDev* __restrict__ draws,
+                                              const FrameDev* __restrict__ frames, Scratch s) {
+    const uint32_t lane = lane_id();
+    const uint32_t nq = min(*(volatile unsigned int*)s.clip_n, (unsigned int)s.clip_list_cap);
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < nq; e += nwarps) {
+        const uint32_t di = s.clip_list[3ull * e], tri = s.clip_list[3ull * e + 1], row = s.clip_list[3ull * e + 2];
+        const DrawDev& d = draws[di];
+        const FrameDev& f = frames[d.frame];
+        ClipVert v;
+        if (lane < 3) {
+            const uint32_t vi = __ldg(d.idx + 3ull * tri + lane);
+            const float4 c = s.vclip[d.vbase + vi];
+            v.p[0] = c.x;
+            v.p[1] = c.y;
+            v.p[2] = c.z;
+            v.p[3] = c.w;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v.a[q] = d.rgba ? __ldg(d.rgba + 4ull * vi + q) : 0.0f;
+            v.a[4] = __ldg(d.uv + 2ull * vi);
+            v.a[5] = __ldg(d.uv + 2ull * vi + 1);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v.p[k] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) v.a[k] = 0.0f;
+        }
+        const int n = warp_clip(v, 3);
+        if (n < 0) {
+            if (lane == 0) atomicOr(s.status, ST_CLIP_OVERFLOW);
+            continue;
+        }
+        if (n < 3) continue;
+        const unsigned long long need = 1ull + 10ull * (unsigned long long)n;
+        unsigned long long off = 0;
+        if (lane == 0) off = atomicAdd(s.clip_used, need);
+        off = __shfl_sync(0xFFFFFFFFu, off, 0);
+        if (off + need > s.clip_cap) {
+            if (lane == 0) atomicOr(s.status, ST_CLIP_STORE_OVERFLOW);
+            continue;
+        }
+        float* st = s.clip_store + off;
+        const float4 sc = to_screen(make_float4(v.p[0], v.p[1], v.p[2], v.p[3]), (float)f.width, (float)f.height);
+        if (lane == 0) st[0] = __int_as_float(n);
+        if (lane < (uint32_t)n) {
+            float* o = st + 1 + 10 * lane;
+            o[0] = sc.x;
+            o[1] = sc.y;
+            o[2] = sc.z;
+            o[3] = sc.w;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) o[4 + q] = v.a[q];
+        }
+        // fan triangle `lane`: vertices 0, lane + 1, lane + 2
+        float4 tv[3];
+        tv[0] = make_float4(__shfl_sync(0xFFFFFFFFu, sc.x, 0), __shfl_sync(0xFFFFFFFFu, sc.y, 0),
+                            __shfl_sync(0xFFFFFFFFu, sc.z, 0), __shfl_sync(0xFFFFFFFFu, sc.w, 0));
+        const uint32_t l1 = min(lane + 1, 31u), l2 = min(lane + 2, 31u);
+        tv[1] = make_float4(__shfl_sync(0xFFFFFFFFu, sc.x, l1), __shfl_sync(0xFFFFFFFFu, sc.y, l1),
+                            __shfl_sync(0xFFFFFFFFu, sc.z, l1), __shfl_sync(0xFFFFFFFFu, sc.w, l1));
+        tv[2] = make_float4(__shfl_sync(0xFFFFFFFFu, sc.x, l2), __shfl_sync(0xFFFFFFFFu, sc.y, l2),
+                            __shfl_sync(0xFFFFFFFFu, sc.z, l2), __shfl_sync(0xFFFFFFFFu, sc.w, l2));
+        uint32_t a0 = 0xFFFFFFFFu, a1 = 0, b0 = 0xFFFFFFFFu, b1 = 0;
+        if (lane + 2 < (uint32_t)n) {
+            uint32_t x0, x1, y0, y1;
+            pixel_bbox(tv, f.width, f.height, x0, x1, y0, y1);
+            if (x0 < x1 && y0 < y1) {
+                a0 = x0;
+                a1 = x1;
+                b0 = y0;
+                b1 = y1;
+            }
+        }
+        a0 = __reduce_min_sync(0xFFFFFFFFu, a0);
+        a1 = __reduce_max_sync(0xFFFFFFFFu, a1);
+        b0 = __reduce_min_sync(0xFFFFFFFFu, b0);
+        b1 = __reduce_max_sync(0xFFFFFFFFu, b1);
+        if (a0 >= a1 || b0 >= b1) continue;
+        const unsigned long long rect = pack_rect(a0, b0, a1 - 1, b1 - 1);
+        const uint32_t g = f.rect_base + d.tbase + tri;
+        if (lane == 0) {
+            s.tri_rect[g] = rect;
+            s.tri_aux[g] = (uint32_t)off;
+        }
+        uint32_t x0, y0, x1, y1;
+        tile_rect(rect, (uint32_t)f.ts, x0, y0, x1, y1);
+        const uint32_t w = x1 - x0 + 1, nt = (y1 - y0 + 1) * w;
+        uint32_t* crow = s.counts + f.count_base + (unsigned long long)row * f.ntiles;
+        for (uint32_t k = lane; k < nt; k += 32) atomicAdd(&crow[(y0 + k / w) * f.tiles_x + x0 + k % w], 1u);
+    }
 }
 
 // ===================================================================== binning: count
@@ -266,7 +343,7 @@ __global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ 
         const uint32_t tri = ch.tri_begin + i;
         unsigned long long rect;
         uint32_t aux;
-        classify_triangle(d, f, tri, s, rect, aux);
+        classify_triangle(d, f, ch.draw, tri, ch.row, s, rect, aux);
         const uint32_t g = f.rect_base + d.tbase + tri;
         s.tri_rect[g] = rect;
         s.tri_aux[g] = aux;
@@ -1458,6 +1535,16 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
         configured = bytes;
     }
     k_bin_count<<<a.nchunks, 256, bytes, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
+    // the straddling triangles the count queued: a grid-stride pass, one warp per triangle
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const uint32_t grid = a.nchunks < (uint32_t)(4 * sms) ? a.nchunks : (uint32_t)(4 * sms);
+    k_clip<<<grid, 256, 0, a.stream>>>(a.draws, a.frames, a.scratch);
     return cudaGetLastError();
 }
 
@@ -1513,6 +1600,7 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
     float* fo = reinterpret_cast<float*>(out);
     uint32_t* uo = reinterpret_cast<uint32_t*>(out);
     const int32_t* ii = reinterpret_cast<const int32_t*>(in);
+    if (op != 5 && threadIdx.x != 0) return;
     switch (op) {
         case 0: {  // perspective divide of 3 clip vertices
             for (int v = 0; v < 3; ++v) {
@@ -1588,29 +1676,33 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
             break;
         }
         case 5: {  // try_clip: in {verts[12], attrs[18]}; out {i32 result, i32 ntris, verts[ntris*12]}
-            ClipVert v3[3];
-            for (int v = 0; v < 3; ++v) {
-                for (int k = 0; k < 4; ++k) v3[v].p[k] = fi[4 * v + k];
-                for (int k = 0; k < 6; ++k) v3[v].a[k] = fi[12 + 6 * v + k];
-            }
+            // the product path's warp clipper (k_clip): the whole warp runs this op
+            const uint32_t lane = lane_id();
+            ClipVert v;
+            for (int k = 0; k < 4; ++k) v.p[k] = lane < 3 ? fi[4 * lane + k] : 0.0f;
+            for (int k = 0; k < 6; ++k) v.a[k] = lane < 3 ? fi[12 + 6 * lane + k] : 0.0f;
             uint32_t codes[3];
-            for (int v = 0; v < 3; ++v)
-                codes[v] = clip_code(make_float4(v3[v].p[0], v3[v].p[1], v3[v].p[2], v3[v].p[3]));
-            int cls = clip_classify(tri2x_area(v3[0].p[0], v3[0].p[1], v3[1].p[0], v3[1].p[1], v3[2].p[0], v3[2].p[1]),
-                                    codes[0], codes[1], codes[2]);
+            for (int q = 0; q < 3; ++q)
+                codes[q] = clip_code(make_float4(fi[4 * q], fi[4 * q + 1], fi[4 * q + 2], fi[4 * q + 3]));
+            int cls = clip_classify(tri2x_area(fi[0], fi[1], fi[4], fi[5], fi[8], fi[9]), codes[0], codes[1], codes[2]);
             int32_t* io = reinterpret_cast<int32_t*>(out);
+            const int n = cls == 2 ? warp_clip(v, 3) : 0;
+            // gather the polygon's positions to lane 0's view through shared memory
+            __shared__ float poly[kMaxPoly][4];
+            if (cls == 2 && n > 0 && lane < (uint32_t)n)
+                for (int k = 0; k < 4; ++k) poly[lane][k] = v.p[k];
+            __syncwarp();
+            if (lane != 0) break;
             io[1] = 0;
             if (cls == 2) {
-                ClipVert poly[kMaxPoly];
-                int n = clip_polygon(v3, poly);
                 if (n < 3) {
                     cls = 0;
                 } else {
                     io[1] = n - 2;
                     for (int t = 0; t + 2 < n; ++t) {
-                        const ClipVert* tv[3] = {&poly[0], &poly[t + 1], &poly[t + 2]};
+                        const int vi[3] = {0, t + 1, t + 2};
                         for (int q = 0; q < 3; ++q)
-                            for (int k = 0; k < 4; ++k) fo[2 + (3 * t + q) * 4 + k] = tv[q]->p[k];
+                            for (int k = 0; k < 4; ++k) fo[2 + (3 * t + q) * 4 + k] = poly[vi[q]][k];
                     }
                 }
             }
@@ -1653,7 +1745,8 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
 }
 
 cudaError_t launch_kat(int op, const void* in, void* out, cudaStream_t stream) {
-    k_kat<<<1, 1, 0, stream>>>(op, static_cast<const unsigned char*>(in), static_cast<unsigned char*>(out));
+    // one warp: op 5 (the warp clipper) uses every lane, the others run on lane 0
+    k_kat<<<1, 32, 0, stream>>>(op, static_cast<const unsigned char*>(in), static_cast<unsigned char*>(out));
     return cudaGetLastError();
 }
 

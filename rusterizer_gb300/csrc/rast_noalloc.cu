@@ -153,6 +153,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     const size_t o_qcount = c.take(split ? sizeof(uint32_t) * 4ull * F.ntiles : 0);
     const size_t clip_floats = 32ull * ntris + 4096ull;
     const size_t o_clip = c.take(sizeof(float) * clip_floats);
+    const size_t o_clist = c.take(sizeof(uint32_t) * 3ull * (ntris ? ntris : 1));
     if (c.off > kNoAllocScratchBytes) return RAST_INVALID_ARG;
 
     unsigned char* base = nullptr;
@@ -217,6 +218,9 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     S.clip_store = reinterpret_cast<float*>(base + o_clip);
     S.clip_cap = clip_floats;
     S.clip_used = &dstate->clip_used;
+    S.clip_list = reinterpret_cast<uint32_t*>(base + o_clist);
+    S.clip_list_cap = ntris;
+    S.clip_n = &dstate->clip_n;
     S.status = &dstate->status;
     S.stats = dstate->stats;
     S.frame_need = reinterpret_cast<unsigned long long*>(base + o_need);

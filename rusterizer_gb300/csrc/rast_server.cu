@@ -59,7 +59,7 @@ uint64_t footprint_of(const rast_ctx* c, const rast_scene& s, int ts, uint64_t b
     const uint64_t chunks = (m.ntris + cs - 1) / cs;
     const uint64_t bin_cap = std::max<uint64_t>(bins, 4ull * m.ntris + tiles + 1024ull);
     const uint64_t split = raster_edge(ts) < ts ? 16ull * (bin_cap + tiles) : 0ull;
-    return 34ull * m.nverts + 12ull * m.ntris + 4ull * chunks * tiles + 12ull * tiles + 4ull * bin_cap + split +
+    return 34ull * m.nverts + 24ull * m.ntris + 4ull * chunks * tiles + 12ull * tiles + 4ull * bin_cap + split +
            4ull * (32ull * m.ntris + 4096ull) + 4ull * (uint64_t)s.width * s.height + 65536ull;
 }
 

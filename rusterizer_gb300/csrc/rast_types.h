@@ -10,6 +10,8 @@
 //   tri_rect[t] u64   pixel box of triangle t (x0,y0,x1,y1 inclusive, 16 bits each),
 //                     kRectEmpty when culled
 //   tri_aux[t]  u32   offset of the clipped polygon in clip_store, kNone when unclipped
+//   clip_list[] u32×3 triangles that straddle a clip plane (draw, triangle, chunk row), clipped
+//                     afterwards by one warp each (k_clip)
 //   counts[frame][chunk][tile] u32  per-chunk tile histograms, then exclusive prefixes
 //   tile_start / tile_count [tile]  each tile's bin range
 //   bins[]    u32     per-tile lists in submission order: triangle << 5 | clipped << 4 |
@@ -124,6 +126,9 @@ struct Scratch {
     uint32_t* qcount;                   // [4 * tile + quadrant] entries in each quadrant list
     float* clip_store;
     unsigned long long clip_cap;        // floats
+    uint32_t* clip_list;                // triangles needing Sutherland-Hodgman: draw, triangle, chunk row
+    unsigned long long clip_list_cap;   // entries
+    unsigned int* clip_n;
     unsigned long long* clip_used;      // floats allocated this frame
     uint32_t* status;
     unsigned long long* stats;          // StatSlots
