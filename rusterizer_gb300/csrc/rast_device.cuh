@@ -191,6 +191,14 @@ __device__ __forceinline__ float edge_eval(float nx, float ny, float px, float p
     return s;
 }
 
+// edge_eval without the leading 0.0 + : the same value except that an exact zero can come out
+// as -0.0 instead of +0.0, which no edge test (e > 0, e < 0, tie rule) can tell apart. Used
+// where the value only feeds edge_pass.
+__device__ __forceinline__ float edge_eval_test(float nx, float ny, float px, float py, float x, float y) {
+    const float dx = x - px, dy = y - py;
+    return nx * dx + ny * dy;
+}
+
 // EdgeFunctions::inside for one edge (src/rasterizer/mod.rs:148-170): the tie rule for an
 // exactly-zero (or NaN) edge value keys off the normal.
 __device__ __forceinline__ bool edge_pass(float e, float nx, float ny) {
@@ -275,12 +283,24 @@ __device__ __forceinline__ void tex_sample(const uint32_t* __restrict__ tex, uin
                                            const float* inv255, float out[4], bool& oob) {
     float x = u * (float)(uint64_t)(tw - 1);
     float y = v * (float)(uint64_t)(th - 1);
-    uint64_t xf = sat_u64(floorf(x)), xc = sat_u64(ceilf(x));
-    uint64_t yf = sat_u64(floorf(y)), yc = sat_u64(ceilf(y));
-    uint32_t tl = read_texel(tex, tw, th, xf, yf, oob);
-    uint32_t tr = read_texel(tex, tw, th, xc, yf, oob);
-    uint32_t bl = read_texel(tex, tw, th, xf, yc, oob);
-    uint32_t br = read_texel(tex, tw, th, xc, yc, oob);
+    uint32_t tl, tr, bl, br;
+    if (x >= 0.0f && y >= 0.0f && x <= (float)(tw - 1) && y <= (float)(th - 1) && tw < 65536u && th < 65536u) {
+        // inside the texture (every in-range uv): floor/ceil stay below the size, so there is no
+        // row wrap or read past the end, and the flat index x + y * w fits 32 bits
+        const uint32_t xf = (uint32_t)floorf(x), xc = (uint32_t)ceilf(x);
+        const uint32_t yf = (uint32_t)floorf(y), yc = (uint32_t)ceilf(y);
+        tl = __ldg(tex + xf + yf * tw);
+        tr = __ldg(tex + xc + yf * tw);
+        bl = __ldg(tex + xf + yc * tw);
+        br = __ldg(tex + xc + yc * tw);
+    } else {
+        uint64_t xf = sat_u64(floorf(x)), xc = sat_u64(ceilf(x));
+        uint64_t yf = sat_u64(floorf(y)), yc = sat_u64(ceilf(y));
+        tl = read_texel(tex, tw, th, xf, yf, oob);
+        tr = read_texel(tex, tw, th, xc, yf, oob);
+        bl = read_texel(tex, tw, th, xf, yc, oob);
+        br = read_texel(tex, tw, th, xc, yc, oob);
+    }
     float x_f = x - truncf(x);
     float y_f = y - truncf(y);
     float omx = 1.0f - x_f, omy = 1.0f - y_f;

@@ -1303,7 +1303,7 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
 #pragma unroll
                     for (int k = 0; k < S; ++k) {
                         const float xs = fx + sample_dx<S>(k), ys = fy + sample_dy<S>(k);
-                        const float e0 = edge_eval(n0x, n0y, p0x, p0y, xs, ys);
+                        const float e0 = edge_eval_test(n0x, n0y, p0x, p0y, xs, ys);
                         const float e1 = edge_eval(n1x, n1y, p1x, p1y, xs, ys);
                         const float e2 = edge_eval(n2x, n2y, p2x, p2y, xs, ys);
                         e1s[k] = e1;
@@ -1403,55 +1403,56 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     }
 }
 
-// Splits each 32-pixel bin of a raster launch into its four quadrant lists, keeping submission
-// order within each (an entry goes to every quadrant its mask names). One CTA per bin; the
-// quadrant raster CTAs then read only their own entries.
+// Splits each 32-pixel bin with entries into its four quadrant lists, keeping submission
+// order within each (an entry goes to every quadrant its mask names). Persistent CTAs walk the
+// bins with entries in the raster queue's order (k_tile_order runs first); the quadrant raster
+// CTAs then read only their own entries.
 __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ frames, int nframes,
-                                                   uint32_t tile0, Scratch s) {
+                                                   const uint32_t* __restrict__ order,
+                                                   const unsigned int* __restrict__ queue, Scratch s) {
     __shared__ uint32_t wcnt[4][8];
     __shared__ uint32_t base[4];
-    const uint32_t gt = tile0 + blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-    const bool overflow = (*(volatile const uint32_t*)s.status & ST_BIN_OVERFLOW) != 0;
-    const uint32_t n = overflow ? 0u : s.tile_count[gt];
-    if (threadIdx.x < 4) {
-        s.qcount[4ull * gt + threadIdx.x] = 0;
-        base[threadIdx.x] = 0;
-    }
-    if (n == 0) return;
-    const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
-    const unsigned long long start = s.tile_start[gt];
-    const uint32_t* src = s.bins + f.bin_base + start;
-    uint32_t* dst = s.qbins + f.qbin_base + 4ull * start;
-    __syncthreads();
-    for (uint32_t e0 = 0; e0 < n; e0 += blockDim.x) {
-        const uint32_t e = e0 + threadIdx.x;
-        const uint32_t ent = e < n ? src[e] : 0u;
-        uint32_t rank[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t b = __ballot_sync(0xFFFFFFFFu, (ent >> q) & 1u);
-            rank[q] = __popc(b & lanemask_lt());
-            if (lane == 0) wcnt[q][warp] = __popc(b);
-        }
+    const uint32_t nbusy = *(volatile const unsigned int*)&queue[2];
+    for (uint32_t qi = blockIdx.x; qi < nbusy; qi += gridDim.x) {
+        const uint32_t gt = order[qi];
+        const uint32_t n = s.tile_count[gt];
+        const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
+        const unsigned long long start = s.tile_start[gt];
+        const uint32_t* src = s.bins + f.bin_base + start;
+        uint32_t* dst = s.qbins + f.qbin_base + 4ull * start;
+        if (threadIdx.x < 4) base[threadIdx.x] = 0;
         __syncthreads();
+        for (uint32_t e0 = 0; e0 < n; e0 += blockDim.x) {
+            const uint32_t e = e0 + threadIdx.x;
+            const uint32_t ent = e < n ? src[e] : 0u;
+            uint32_t rank[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if ((ent >> q) & 1u) {
-                uint32_t off = base[q] + rank[q];
-                for (uint32_t w = 0; w < warp; ++w) off += wcnt[q][w];
-                dst[(unsigned long long)q * n + off] = ent;
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t bq = __ballot_sync(0xFFFFFFFFu, (ent >> q) & 1u);
+                rank[q] = __popc(bq & lanemask_lt());
+                if (lane == 0) wcnt[q][warp] = __popc(bq);
             }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if ((ent >> q) & 1u) {
+                    uint32_t off = base[q] + rank[q];
+                    for (uint32_t w = 0; w < warp; ++w) off += wcnt[q][w];
+                    dst[(unsigned long long)q * n + off] = ent;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 4) {
+                uint32_t t = 0;
+                for (uint32_t w = 0; w < blockDim.x / 32; ++w) t += wcnt[threadIdx.x][w];
+                base[threadIdx.x] += t;
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        if (threadIdx.x < 4) {
-            uint32_t t = 0;
-            for (uint32_t w = 0; w < blockDim.x / 32; ++w) t += wcnt[threadIdx.x][w];
-            base[threadIdx.x] += t;
-        }
+        if (threadIdx.x < 4) s.qcount[4ull * gt + threadIdx.x] = base[threadIdx.x];
         __syncthreads();
     }
-    if (threadIdx.x < 4) s.qcount[4ull * gt + threadIdx.x] = base[threadIdx.x];
 }
 
 // Tile queue of one raster launch: tiles with entries first, in decreasing order of entry
@@ -1506,11 +1507,14 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         grid_cap = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
-    if (nsx > 1)
-        k_bin_split<<<a.raster_blocks, 256, 0, a.stream>>>(a.raster_frames, a.raster_nframes,
-                                                           a.raster_tile_offset, a.scratch);
     k_tile_order<<<1, 1024, 0, a.stream>>>(a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
                                            a.scratch.tile_order, a.raster_queue, a.scratch.status);
+    if (nsx > 1) {
+        const unsigned sgrid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
+        k_bin_split<<<sgrid, 256, 0, a.stream>>>(a.raster_frames, a.raster_nframes,
+                                                 a.scratch.tile_order + a.raster_tile_offset, a.raster_queue,
+                                                 a.scratch);
+    }
     const unsigned long long units = (unsigned long long)a.raster_blocks * nsx * nsx;
     const unsigned grid = units < (unsigned long long)grid_cap ? (unsigned)units : (unsigned)grid_cap;
     k_raster<S, TS><<<grid, kRasterThreads, bytes, a.stream>>>(
