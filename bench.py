@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
            1: "triangle soup 100k tris 1920x1080 4xMSAA",
            2: "heightfield 2M tris 3840x2160 4xMSAA"}
-LAUNCHES_PER_FRAME = 7  # vertex, bin count, column scan, tile scan, scatter, tile order, raster
+LAUNCHES_PER_FRAME = 8  # vertex, bin count, clip, column scan, tile scan, scatter, tile order, raster
 
 
 def make_scene(cfg):
@@ -517,7 +517,7 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--nscenes", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+",
-                    default=[250, 500, 1000, 2000, 4000, 8000, 16000, 32000])
+                    default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 10000, 12000, 16000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--p99-bound-ms", type=float, default=50.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
