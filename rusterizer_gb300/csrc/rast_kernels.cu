@@ -1468,9 +1468,12 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
     __syncthreads();
     // after a bin overflow every tile is cleared and the host re-runs the frame
     const bool overflow = (*(volatile const uint32_t*)status & ST_BIN_OVERFLOW) != 0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const uint32_t c = overflow ? 0u : tile_count[tile0 + i];
-        atomicAdd(&cnt[32 - __clz(c)], 1u);
+    // lanes with the same bucket add once per warp (thousands of tiles share a few buckets)
+    for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        const uint32_t b = i < n ? 32 - __clz(overflow ? 0u : tile_count[tile0 + i]) : 33u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
+        if (b < 33u && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[b], (uint32_t)__popc(peers));
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1482,10 +1485,15 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
         queue[2] = n - cnt[0];
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const uint32_t c = overflow ? 0u : tile_count[tile0 + i];
-        const uint32_t pos = atomicAdd(&off[32 - __clz(c)], 1u);
-        order[tile0 + pos] = tile0 + i;
+    for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        const uint32_t b = i < n ? 32 - __clz(overflow ? 0u : tile_count[tile0 + i]) : 33u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (b < 33u && lane_id() == leader) base = atomicAdd(&off[b], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (b < 33u) order[tile0 + base + __popc(peers & lanemask_lt())] = tile0 + i;
     }
 }
 
