@@ -681,6 +681,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 
 constexpr int kRasterThreads = 256;
 constexpr int kRasterWarps = kRasterThreads / 32;
+constexpr int kEmptyRun = 8;  // bins without entries taken per queue update
 
 // A raster CTA owns one TS x TS tile: a whole bin (bin edge == TS) or one quadrant of a bin
 // twice as wide. Bin entries carry, in their low 4 bits, the quadrants the triangle's pixel box
@@ -1080,6 +1081,21 @@ __device__ __forceinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, ui
 __device__ __forceinline__ void clear_tile_warp(const FrameDev& f, uint32_t x0, uint32_t y0,
                                                 uint32_t edge, int S) {
     const uint32_t lane = lane_id();
+    if (!f.dbg_depth && (f.width & 3u) == 0 && x0 + edge <= f.width &&
+        (reinterpret_cast<uintptr_t>(f.out) & 15u) == 0) {
+        // whole rows of 16-byte stores: the image starts on a 16-byte boundary (checked; batch
+        // outputs can start anywhere), width % 4 == 0 and x0 is a multiple of the bin edge, so
+        // every row segment does too
+        const uint32_t q = edge / 4, sh = __ffs(q) - 1;  // uint4 per row (2, 4 or 8), its log2
+        const uint4 c = make_uint4(kClearColor, kClearColor, kClearColor, kClearColor);
+        for (uint32_t i = lane; i < edge * q; i += 32) {
+            const uint32_t y = y0 + (i >> sh);
+            if (y >= f.height) break;
+            uint4* row = reinterpret_cast<uint4*>(f.out + (unsigned long long)y * f.width + x0);
+            row[i & (q - 1)] = c;
+        }
+        return;
+    }
     for (uint32_t i = lane; i < edge * edge; i += 32) {
         const uint32_t x = x0 + i % edge, y = y0 + i / edge;
         if (x >= f.width || y >= f.height) continue;
@@ -1369,17 +1385,21 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     }
     }  // units with entries
 
-    // ---- bins without entries: warps take whole bins and write the clear colour
+    // ---- bins without entries: warps take runs of kEmptyRun bins (one counter update per run,
+    // not per bin) and write the clear colour
     for (;;) {
-        uint32_t qi = 0;
-        if (lane == 0) qi = atomicAdd(&queue[1], 1u);
-        qi = __shfl_sync(0xFFFFFFFFu, qi, 0) + nbusy;
-        if (qi >= ntotal) break;
-        const uint32_t gt = order[qi];
-        const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
-        const uint32_t lt = gt - f.tile_begin;
-        const uint32_t edge = (uint32_t)f.ts;
-        clear_tile_warp(f, (lt % f.tiles_x) * edge, (lt / f.tiles_x) * edge, edge, S);
+        uint32_t q0 = 0;
+        if (lane == 0) q0 = atomicAdd(&queue[1], (unsigned)kEmptyRun);
+        q0 = __shfl_sync(0xFFFFFFFFu, q0, 0) + nbusy;
+        if (q0 >= ntotal) break;
+        const uint32_t q1 = min(q0 + (uint32_t)kEmptyRun, ntotal);
+        for (uint32_t qi = q0; qi < q1; ++qi) {
+            const uint32_t gt = order[qi];
+            const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
+            const uint32_t lt = gt - f.tile_begin;
+            const uint32_t edge = (uint32_t)f.ts;
+            clear_tile_warp(f, (lt % f.tiles_x) * edge, (lt / f.tiles_x) * edge, edge, S);
+        }
     }
     // per-block statistics
     __syncthreads();
