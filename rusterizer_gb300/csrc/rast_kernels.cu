@@ -1134,8 +1134,10 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     const uint32_t nbusy = *(volatile unsigned int*)&queue[2];  // written by k_tile_order
     const uint32_t nsub = nsx * nsx;
 
-    for (;;) {
+    // unit tickets (heaviest first); the next one is taken when the current unit starts its
+    // resolve, so the queue update is in flight during the resolve
     if (threadIdx.x == 0) sm.misc[0] = atomicAdd(&queue[0], 1u);
+    for (;;) {
     __syncthreads();
     const uint32_t qi = sm.misc[0];
     __syncthreads();
@@ -1367,6 +1369,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
 
     // ---- resolve (resolve_and_clear + box_filter_color, mod.rs:478-518, buffers.rs:111-125)
     __syncthreads();
+    uint32_t next_ticket = 0;
+    if (threadIdx.x == 0) next_ticket = atomicAdd(&queue[0], 1u);
     for (uint32_t p = threadIdx.x; p < (uint32_t)C::NPIX; p += blockDim.x) {
         const uint32_t x = X0 + p % TS, y = Y0 + p / TS;
         if (x >= W || y >= H) continue;
@@ -1383,6 +1387,7 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             }
         }
     }
+    if (threadIdx.x == 0) sm.misc[0] = next_ticket;
     }  // units with entries
 
     // ---- bins without entries: warps take runs of kEmptyRun bins (one counter update per run,
