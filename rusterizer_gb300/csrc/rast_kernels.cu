@@ -34,14 +34,15 @@ __device__ __forceinline__ void unpack_rect(unsigned long long r, uint32_t& x0, 
     x1 = (uint32_t)((r >> 32) & 0xFFFFu);
     y1 = (uint32_t)((r >> 48) & 0xFFFFu);
 }
-// Tile rectangle (inclusive) of a pixel box (inclusive) for tiles of edge ts.
+// Tile rectangle (inclusive) of a pixel box (inclusive) for tiles of edge ts (a power of two).
 __device__ __forceinline__ void tile_rect(unsigned long long r, uint32_t ts, uint32_t& x0, uint32_t& y0,
                                           uint32_t& x1, uint32_t& y1) {
     unpack_rect(r, x0, y0, x1, y1);
-    x0 /= ts;
-    y0 /= ts;
-    x1 /= ts;
-    y1 /= ts;
+    const uint32_t sh = __ffs(ts) - 1;
+    x0 >>= sh;
+    y0 >>= sh;
+    x1 >>= sh;
+    y1 >>= sh;
 }
 __device__ __forceinline__ uint32_t rect_tiles(unsigned long long r, uint32_t ts) {
     if (r == kRectEmpty) return 0;
@@ -59,12 +60,12 @@ __device__ __forceinline__ uint32_t bin_entry(uint32_t tri, bool clipped, unsign
     if (rs == ts) return head | 1u;
     uint32_t px0, py0, px1, py1;
     unpack_rect(r, px0, py0, px1, py1);
-    const uint32_t ox = tx * ts, oy = ty * ts;
-    const uint32_t sx0 = (max(px0, ox) - ox) / rs, sx1 = (min(px1, ox + ts - 1) - ox) / rs;
-    const uint32_t sy0 = (max(py0, oy) - oy) / rs, sy1 = (min(py1, oy + ts - 1) - oy) / rs;
+    const uint32_t ox = tx * ts, oy = ty * ts, rsh = __ffs(rs) - 1, nsx = ts >> rsh;
+    const uint32_t sx0 = (max(px0, ox) - ox) >> rsh, sx1 = (min(px1, ox + ts - 1) - ox) >> rsh;
+    const uint32_t sy0 = (max(py0, oy) - oy) >> rsh, sy1 = (min(py1, oy + ts - 1) - oy) >> rsh;
     uint32_t m = 0;
     for (uint32_t sy = sy0; sy <= sy1; ++sy)
-        for (uint32_t sx = sx0; sx <= sx1; ++sx) m |= 1u << (sy * (ts / rs) + sx);
+        for (uint32_t sx = sx0; sx <= sx1; ++sx) m |= 1u << (sy * nsx + sx);
     return head | m;
 }
 
@@ -460,7 +461,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     __shared__ uint32_t hkey[kHashSlots];
     __shared__ uint16_t wcnt[kHashSlots][kScatterWarps];
     __shared__ uint16_t slot_list[kPairsPerBatch];
-    __shared__ uint16_t ptile[kPairsPerBatch], pslot[kPairsPerBatch], prank[kPairsPerBatch];
+    __shared__ uint32_t pxy[kPairsPerBatch];  // tile x | tile y << 16
+    __shared__ uint16_t pslot[kPairsPerBatch], prank[kPairsPerBatch];
     __shared__ uint16_t ptri[kPairsPerBatch];
     __shared__ unsigned long long trect[kScatterWindow];
     __shared__ uint32_t tclip[kScatterWindow / 32];
@@ -587,7 +589,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             const uint32_t src = min(sl, 31u);
             const uint32_t o = pi - __shfl_sync(0xFFFFFFFFu, winc - pc, src);
             const uint32_t n0 = __shfl_sync(0xFFFFFFFFu, n[0], src);
-            uint32_t key = 0xFFFFFFFFu - lane, v = 0;
+            uint32_t key = 0xFFFFFFFFu - lane, v = 0, xy = 0;
             if (pi < wtotal) {
                 const uint32_t j = o < n0 ? 0u : 1u, k = o < n0 ? o : o - n0;
                 v = (warp * 32 + src) * kScatterTriPerThread + j;
@@ -595,7 +597,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                 tile_rect(trect[v], ts, x0, y0, x1, y1);
                 const uint32_t w = x1 - x0 + 1;
                 const uint32_t ky = k < w ? 0u : k / w;
-                key = (y0 + ky) * tx + x0 + (k - ky * w);
+                const uint32_t ttx = x0 + (k - ky * w), tty = y0 + ky;
+                key = tty * tx + ttx;
+                xy = ttx | (tty << 16);
             }
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
             const uint32_t leader = __ffs(peers) - 1;
@@ -619,7 +623,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             old = __shfl_sync(0xFFFFFFFFu, old, leader);
             if (pi < wtotal) {
                 const uint32_t bp = wbase + pi;
-                ptile[bp] = (uint16_t)key;
+                pxy[bp] = xy;
                 pslot[bp] = (uint16_t)slot;
                 prank[bp] = (uint16_t)(old + __popc(peers & lanemask_lt()));
                 ptri[bp] = (uint16_t)v;
@@ -649,13 +653,14 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         __syncthreads();
         npairs = tmp[0];
         for (uint32_t bp = threadIdx.x; bp < npairs; bp += blockDim.x) {
-            const uint32_t t = ptile[bp], slot = pslot[bp], v = ptri[bp];
+            const uint32_t xy = pxy[bp], slot = pslot[bp], v = ptri[bp];
+            const uint32_t ttx = xy & 0xFFFFu, tty = xy >> 16, t = tty * tx + ttx;
             const uint32_t pw = v / (32 * kScatterTriPerThread);
             uint32_t before = prank[bp];
             for (uint32_t w2 = 0; w2 < pw; ++w2) before += wcnt[slot][w2];
             const uint32_t pos = run_off[t] + before;
             const bool clipped = (tclip[v >> 5] >> (v & 31u)) & 1u;
-            if (pos < cap) bins[pos] = bin_entry(fbase + base + v, clipped, trect[v], t % tx, t / tx, ts);
+            if (pos < cap) bins[pos] = bin_entry(fbase + base + v, clipped, trect[v], ttx, tty, ts);
         }
         __syncthreads();
         const uint32_t ns = nslots;
