@@ -209,6 +209,11 @@ __device__ __forceinline__ bool edge_pass(float e, float nx, float ny) {
     return ny < 0.0f;
 }
 
+// The same edge test with the tie rule precomputed (edge_tie) and no branches: pass when the
+// value is positive, or when it is zero or NaN and the tie rule holds.
+__device__ __forceinline__ bool edge_tie(float nx, float ny) { return (nx > 0.0f) | (!(nx < 0.0f) & (ny < 0.0f)); }
+__device__ __forceinline__ bool edge_pass_t(float e, bool tie) { return (e > 0.0f) | (!(e < 0.0f) & tie); }
+
 // RasterizerTriangle::fragment's interpolate_depth (src/rasterizer/mod.rs:226-236)
 __device__ __forceinline__ float interp_depth(float e1, float e2, float inv, float z0, float z1,
                                               float z2) {

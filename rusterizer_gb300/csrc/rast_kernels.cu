@@ -1322,24 +1322,21 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                     const float p0x = sm.ipx[0][it], p0y = sm.ipy[0][it];
                     const float p1x = sm.ipx[1][it], p1y = sm.ipy[1][it];
                     const float p2x = sm.ipx[2][it], p2y = sm.ipy[2][it];
-                    float e1s[S], e2s[S];
+                    // tie rule per edge (EdgeFunctions::inside, mod.rs:148-170), once per pixel
+                    const bool t0 = edge_tie(n0x, n0y), t1 = edge_tie(n1x, n1y), t2 = edge_tie(n2x, n2y);
+                    const float inv = sm.iinv[it];
+                    const float z0 = sm.iz[0][it], z1 = sm.iz[1][it], z2 = sm.iz[2][it];
 #pragma unroll
                     for (int k = 0; k < S; ++k) {
                         const float xs = fx + sample_dx<S>(k), ys = fy + sample_dy<S>(k);
                         const float e0 = edge_eval_test(n0x, n0y, p0x, p0y, xs, ys);
                         const float e1 = edge_eval(n1x, n1y, p1x, p1y, xs, ys);
                         const float e2 = edge_eval(n2x, n2y, p2x, p2y, xs, ys);
-                        e1s[k] = e1;
-                        e2s[k] = e2;
-                        if (edge_pass(e0, n0x, n0y) && edge_pass(e1, n1x, n1y) && edge_pass(e2, n2x, n2y))
-                            cov |= 1u << k;
-                    }
-                    if (cov) {
-                        const float inv = sm.iinv[it];
-                        const float z0 = sm.iz[0][it], z1 = sm.iz[1][it], z2 = sm.iz[2][it];
-#pragma unroll
-                        for (int k = 0; k < S; ++k)
-                            if ((cov >> k) & 1u) z[k] = interp_depth(e1s[k], e2s[k], inv, z0, z1, z2);
+                        // branch-free: every sample's depth is computed, the covered ones kept
+                        const bool in = edge_pass_t(e0, t0) & edge_pass_t(e1, t1) & edge_pass_t(e2, t2);
+                        const float zk = interp_depth(e1, e2, inv, z0, z1, z2);
+                        cov |= (uint32_t)in << k;
+                        z[k] = in ? zk : 0.0f;
                     }
                 }
                 const uint32_t bal = __ballot_sync(0xFFFFFFFFu, cov != 0);
