@@ -240,17 +240,17 @@ __device__ __forceinline__ float sample_dy(int i) {
 template <int S>
 __device__ __forceinline__ void interp_point(uint32_t x, uint32_t y, uint32_t dm, float& xs,
                                              float& ys) {
-    xs = (float)x + 0.5f;
-    ys = (float)y + 0.5f;
-    if (dm != (1u << S) - 1u) {
+    // offsets of the first passed sample, selected without branches
+    const int i = __ffs(dm) - 1;
+    float dx = 0.5f, dy = 0.5f;
 #pragma unroll
-        for (int i = 0; i < S; ++i)
-            if (dm & (1u << i)) {
-                xs = (float)x + sample_dx<S>(i);
-                ys = (float)y + sample_dy<S>(i);
-                break;
-            }
+    for (int k = 0; k < S; ++k) {
+        dx = i == k ? sample_dx<S>(k) : dx;
+        dy = i == k ? sample_dy<S>(k) : dy;
     }
+    const bool all = dm == (1u << S) - 1u;
+    xs = (float)x + (all ? 0.5f : dx);
+    ys = (float)y + (all ? 0.5f : dy);
 }
 
 // Perspective-correct barycentrics of Fragment::interpolate (src/rasterizer/mod.rs:85-94).

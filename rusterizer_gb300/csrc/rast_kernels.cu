@@ -987,17 +987,18 @@ __device__ __forceinline__ void warp_depth(RasterSmem<S, TS>& sm, uint32_t w, ui
     const uint32_t maxr = __reduce_max_sync(0xFFFFFFFFu, rank);
     uint32_t dm = 0;
     for (uint32_t r = 0; r <= maxr; ++r) {
-        if (valid && rank == r) {
+        // this round's lanes: no two share a pixel; the test and the store are predicated
+        const bool act = valid && rank == r;
 #pragma unroll
-            for (int k = 0; k < S; ++k)
-                if (((cov >> k) & 1u) && z[k] < sm.zb[k * C::NPIX + pix]) {
-                    dm |= 1u << k;
-                    sm.zb[k * C::NPIX + pix] = z[k];
-                }
-            if (s.log)
-                log_fragment(s, sm.itri[it], sm.imeta[it] & 0xFFu, ((Y0 + pix / TS) << 16) | (X0 + pix % TS),
-                             (dm << 8) | cov);
+        for (int k = 0; k < S; ++k) {
+            const float old = sm.zb[k * C::NPIX + pix];
+            const bool pass = act & (((cov >> k) & 1u) != 0) & (z[k] < old);
+            if (pass) sm.zb[k * C::NPIX + pix] = z[k];
+            dm |= (uint32_t)pass << k;
         }
+        if (s.log && act)
+            log_fragment(s, sm.itri[it], sm.imeta[it] & 0xFFu, ((Y0 + pix / TS) << 16) | (X0 + pix % TS),
+                         (dm << 8) | cov);
         __syncwarp();
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, dm != 0);
@@ -1073,11 +1074,10 @@ __device__ __forceinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, ui
     const uint32_t rank = __popc(grp & lanemask_lt());
     const uint32_t maxr = __reduce_max_sync(0xFFFFFFFFu, rank);
     for (uint32_t r = 0; r <= maxr; ++r) {
-        if (valid && rank == r) {
+        const bool act = valid && rank == r;
 #pragma unroll
-            for (int k = 0; k < S; ++k)
-                if ((dm >> k) & 1u) sm.cb[k * C::NPIX + pix] = argb;
-        }
+        for (int k = 0; k < S; ++k)
+            if (act & (((dm >> k) & 1u) != 0)) sm.cb[k * C::NPIX + pix] = argb;
         __syncwarp();
     }
 }
