@@ -235,7 +235,15 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         if (E.profiling) cudaEventRecord(E.ev[3], st);
         if (err == cudaSuccess) err = launch_bin_scatter(a);
         if (E.profiling) cudaEventRecord(E.ev[4], st);
-        // raster: one launch per (msaa, tile) group of consecutive frames
+        // raster: one launch per (msaa, tile) group of consecutive frames; with several groups
+        // (batches of mixed MSAA) they alternate between the context stream and its side stream,
+        // so one group's tail overlaps the next group's start
+        const bool multi = !frames.empty() &&
+                           (frames.front().msaa != frames.back().msaa || frames.front().ts != frames.back().ts);
+        if (multi && err == cudaSuccess) {
+            if (cudaEventRecord(E.fork, st) != cudaSuccess || cudaStreamWaitEvent(E.side, E.fork, 0) != cudaSuccess)
+                err = cudaErrorUnknown;
+        }
         int group = 0;
         for (size_t i = 0; i < frames.size() && err == cudaSuccess; ++group) {
             if (group >= 8) {
@@ -248,6 +256,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
                 blocks += frames[j].ntiles;
                 ++j;
             }
+            a.stream = (multi && (group & 1)) ? E.side : st;
             a.raster_frames = a.frames + i;
             a.raster_nframes = (int)(j - i);
             a.raster_tile_offset = frames[i].tile_begin;
@@ -255,6 +264,11 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
             a.raster_queue = &E.d_state->queue[4 * group];
             err = launch_raster(a, frames[i].msaa, frames[i].ts);
             i = j;
+        }
+        a.stream = st;
+        if (multi && err == cudaSuccess) {
+            if (cudaEventRecord(E.join, E.side) != cudaSuccess || cudaStreamWaitEvent(st, E.join, 0) != cudaSuccess)
+                err = cudaErrorUnknown;
         }
         if (E.profiling) cudaEventRecord(E.ev[5], st);
         if (err != cudaSuccess) return RAST_CUDA_ERROR;

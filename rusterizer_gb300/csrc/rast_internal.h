@@ -208,6 +208,9 @@ struct Engine {
     std::vector<unsigned char> h_scratch;
     std::vector<size_t> h_order;  // job index of each frame of the last launch (device order)
     cudaEvent_t desc_done = nullptr;  // last descriptor upload finished reading h_desc
+    // a second stream for raster launches of different (msaa, tile) groups, which then overlap
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     bool desc_pending = false, desc_valid = false;
     size_t desc_bytes = 0;
     unsigned char* d_desc_ptr = nullptr;
@@ -220,6 +223,9 @@ struct Engine {
         for (auto& e : ev)
             if (cudaEventCreate(&e) != cudaSuccess) return false;
         if (cudaEventCreateWithFlags(&desc_done, cudaEventDisableTiming) != cudaSuccess) return false;
+        if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&join, cudaEventDisableTiming) != cudaSuccess) return false;
         return h_need.reserve(64);
     }
     ~Engine() {
@@ -227,6 +233,10 @@ struct Engine {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (desc_done) cudaEventDestroy(desc_done);
+        if (side) cudaStreamSynchronize(side);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
         if (d_state) cudaFree(d_state);
         if (h_state) cudaFreeHost(h_state);
         if (stream) cudaStreamDestroy(stream);
