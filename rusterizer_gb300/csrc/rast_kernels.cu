@@ -898,7 +898,7 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
 template <int TS>
 __device__ __forceinline__ uint32_t split_work(const int* rowd, const int* cold) {
     const uint32_t lane = lane_id();
-    // per-line work from the difference arrays
+    // per-line work from the difference arrays (lane = line)
     int rw = lane < (uint32_t)TS ? rowd[lane] : 0, cw = lane < (uint32_t)TS ? cold[lane] : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -908,16 +908,20 @@ __device__ __forceinline__ uint32_t split_work(const int* rowd, const int* cold)
             cw += z;
         }
     }
-    const uint32_t wr = lane < (uint32_t)TS ? (uint32_t)rw : 0u;
-    const uint32_t wc = lane < (uint32_t)TS ? (uint32_t)cw : 0u;
-    uint32_t mrow = 0, mcol = 0;
+    uint32_t wr = lane < (uint32_t)TS ? (uint32_t)rw : 0u;
+    uint32_t wc = lane < (uint32_t)TS ? (uint32_t)cw : 0u;
+    // each warp's load: the sum of its lines (lane % kRasterWarps), then the heaviest warp
 #pragma unroll
-    for (int k = 0; k < kRasterWarps; ++k) {
-        const bool mine = (lane % kRasterWarps) == (uint32_t)k;
-        mrow = max(mrow, __reduce_add_sync(0xFFFFFFFFu, mine ? wr : 0u));
-        mcol = max(mcol, __reduce_add_sync(0xFFFFFFFFu, mine ? wc : 0u));
+    for (int o = kRasterWarps; o < 32; o <<= 1) {
+        wr += __shfl_down_sync(0xFFFFFFFFu, wr, o);
+        wc += __shfl_down_sync(0xFFFFFFFFu, wc, o);
     }
-    return mcol < mrow ? 1u : 0u;
+#pragma unroll
+    for (int o = kRasterWarps / 2; o > 0; o >>= 1) {
+        wr = max(wr, __shfl_xor_sync(0xFFFFFFFFu, wr, o));
+        wc = max(wc, __shfl_xor_sync(0xFFFFFFFFu, wc, o));
+    }
+    return wc < wr ? 1u : 0u;  // lane 0's values cover lanes 0 .. kRasterWarps - 1
 }
 
 // Appends one fragment record to the debug log (rast_debug_log_enable); kept out of line.
