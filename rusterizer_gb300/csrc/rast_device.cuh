@@ -193,24 +193,15 @@ __device__ __forceinline__ float edge_eval(float nx, float ny, float px, float p
 
 // edge_eval without the leading 0.0 + : the same value except that an exact zero can come out
 // as -0.0 instead of +0.0, which no edge test (e > 0, e < 0, tie rule) can tell apart. Used
-// where the value only feeds edge_pass.
+// where the value only feeds the edge test.
 __device__ __forceinline__ float edge_eval_test(float nx, float ny, float px, float py, float x, float y) {
     const float dx = x - px, dy = y - py;
     return nx * dx + ny * dy;
 }
 
-// EdgeFunctions::inside for one edge (src/rasterizer/mod.rs:148-170): the tie rule for an
-// exactly-zero (or NaN) edge value keys off the normal.
-__device__ __forceinline__ bool edge_pass(float e, float nx, float ny) {
-    if (e > 0.0f) return true;
-    if (e < 0.0f) return false;
-    if (nx > 0.0f) return true;
-    if (nx < 0.0f) return false;
-    return ny < 0.0f;
-}
-
-// The same edge test with the tie rule precomputed (edge_tie) and no branches: pass when the
-// value is positive, or when it is zero or NaN and the tie rule holds.
+// EdgeFunctions::inside for one edge (src/rasterizer/mod.rs:148-170) without branches: pass
+// when the value is positive, or when it is zero (or NaN) and the tie rule holds; the tie rule
+// keys off the normal: x > 0, or x not negative and y < 0 (edge_tie, once per triangle edge).
 __device__ __forceinline__ bool edge_tie(float nx, float ny) { return (nx > 0.0f) | (!(nx < 0.0f) & (ny < 0.0f)); }
 __device__ __forceinline__ bool edge_pass_t(float e, bool tie) { return (e > 0.0f) | (!(e < 0.0f) & tie); }
 

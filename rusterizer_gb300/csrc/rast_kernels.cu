@@ -1684,7 +1684,7 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
                 float e[3];
                 for (int k = 0; k < 3; ++k) e[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], xs, ys);
                 bool in3 = true;
-                for (int k = 0; k < 3; ++k) in3 = in3 && edge_pass(e[k], t.nx[k], t.ny[k]);
+                for (int k = 0; k < 3; ++k) in3 = in3 && edge_pass_t(e[k], edge_tie(t.nx[k], t.ny[k]));
                 if (in3) {
                     cov |= 1u << q;
                     d[q] = interp_depth(e[1], e[2], t.inv_area, t.z[0], t.z[1], t.z[2]);
@@ -1713,7 +1713,7 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
             bool in3 = true;
             for (int k = 0; k < 3; ++k) {
                 fo[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], fi[9], fi[10]);
-                in3 = in3 && edge_pass(fo[k], t.nx[k], t.ny[k]);
+                in3 = in3 && edge_pass_t(fo[k], edge_tie(t.nx[k], t.ny[k]));
             }
             uo[3] = in3;
             break;
