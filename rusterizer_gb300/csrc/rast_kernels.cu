@@ -1437,13 +1437,15 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
 // Splits each 32-pixel bin with entries into its four quadrant lists, keeping submission
 // order within each (an entry goes to every quadrant its mask names). Persistent CTAs walk the
 // bins with entries in the raster queue's order (k_tile_order runs first); the quadrant raster
-// CTAs then read only their own entries.
+// CTAs then read only their own entries. Windows of 4 consecutive entries per thread; the
+// per-quadrant counts travel as 16-bit fields (two quadrants per word) through one block scan.
 __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ frames, int nframes,
                                                    const uint32_t* __restrict__ order,
                                                    const unsigned int* __restrict__ queue, Scratch s) {
-    __shared__ uint32_t wcnt[4][8];
+    constexpr int kPer = 4;
+    __shared__ uint32_t tmp[2][33];
     __shared__ uint32_t base[4];
-    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t nbusy = *(volatile const unsigned int*)&queue[2];
     for (uint32_t qi = blockIdx.x; qi < nbusy; qi += gridDim.x) {
         const uint32_t gt = order[qi];
@@ -1453,31 +1455,62 @@ __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ 
         const uint32_t* src = s.bins + f.bin_base + start;
         uint32_t* dst = s.qbins + f.qbin_base + 4ull * start;
         if (threadIdx.x < 4) base[threadIdx.x] = 0;
-        __syncthreads();
-        for (uint32_t e0 = 0; e0 < n; e0 += blockDim.x) {
-            const uint32_t e = e0 + threadIdx.x;
-            const uint32_t ent = e < n ? src[e] : 0u;
-            uint32_t rank[4];
+        for (uint32_t e0 = 0; e0 < n; e0 += blockDim.x * kPer) {
+            uint32_t ent[kPer];
+            uint32_t c01 = 0, c23 = 0;  // this thread's count per quadrant, 16 bits each
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const uint32_t bq = __ballot_sync(0xFFFFFFFFu, (ent >> q) & 1u);
-                rank[q] = __popc(bq & lanemask_lt());
-                if (lane == 0) wcnt[q][warp] = __popc(bq);
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t e = e0 + threadIdx.x * kPer + j;
+                ent[j] = e < n ? src[e] : 0u;
+                c01 += (ent[j] & 1u) + (((ent[j] >> 1) & 1u) << 16);
+                c23 += ((ent[j] >> 2) & 1u) + (((ent[j] >> 3) & 1u) << 16);
+            }
+            // block-wide exclusive scan of both words at once
+            uint32_t x01 = c01, x23 = c23;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y01 = __shfl_up_sync(0xFFFFFFFFu, x01, o), y23 = __shfl_up_sync(0xFFFFFFFFu, x23, o);
+                if (lane >= (uint32_t)o) {
+                    x01 += y01;
+                    x23 += y23;
+                }
+            }
+            if (lane == 31) {
+                tmp[0][warp] = x01;
+                tmp[1][warp] = x23;
             }
             __syncthreads();
+            if (warp == 0) {
+                const uint32_t w01 = lane < nw ? tmp[0][lane] : 0u, w23 = lane < nw ? tmp[1][lane] : 0u;
+                uint32_t s01 = w01, s23 = w23;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if ((ent >> q) & 1u) {
-                    uint32_t off = base[q] + rank[q];
-                    for (uint32_t w = 0; w < warp; ++w) off += wcnt[q][w];
-                    dst[(unsigned long long)q * n + off] = ent;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y01 = __shfl_up_sync(0xFFFFFFFFu, s01, o), y23 = __shfl_up_sync(0xFFFFFFFFu, s23, o);
+                    if (lane >= (uint32_t)o) {
+                        s01 += y01;
+                        s23 += y23;
+                    }
+                }
+                tmp[0][lane] = s01 - w01;
+                tmp[1][lane] = s23 - w23;
+                if (lane == 31) {
+                    tmp[0][32] = s01;
+                    tmp[1][32] = s23;
                 }
             }
             __syncthreads();
+            const uint32_t p01 = tmp[0][warp] + x01 - c01, p23 = tmp[1][warp] + x23 - c23;
+            uint32_t o[4] = {base[0] + (p01 & 0xFFFFu), base[1] + (p01 >> 16), base[2] + (p23 & 0xFFFFu),
+                             base[3] + (p23 >> 16)};
+#pragma unroll
+            for (int j = 0; j < kPer; ++j)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if ((ent[j] >> q) & 1u) dst[(unsigned long long)q * n + o[q]++] = ent[j];
+            __syncthreads();
             if (threadIdx.x < 4) {
-                uint32_t t = 0;
-                for (uint32_t w = 0; w < blockDim.x / 32; ++w) t += wcnt[threadIdx.x][w];
-                base[threadIdx.x] += t;
+                const uint32_t t = tmp[threadIdx.x >> 1][32];
+                base[threadIdx.x] += (threadIdx.x & 1u) ? (t >> 16) : (t & 0xFFFFu);
             }
             __syncthreads();
         }
