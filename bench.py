@@ -137,10 +137,49 @@ def cpu_baseline(scene, seconds, nthreads):
     return n / dt, n, dt, shaded
 
 
+def run_reference_scenes(args):
+    """Reference arm for configs 3 and 4: the oracle renders the batch's scenes one after another
+    (row bands over every host thread); each step renders scenes for up to 5 s. A CPU renderer
+    serves requests at most this fast, so config 4 reports the same rate in requests/s."""
+    import oracle
+    from rusterizer_gb300 import scenes
+    cores = os.cpu_count() or 1
+    specs = scenes.batch_scene_specs(args.nscenes, 3)
+    sc = [scenes.batch_scene(s) for s in specs]
+    oracle.render_scene(sc[0], nthreads=cores)
+    n = 0
+    t_all = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        while True:
+            oracle.render_scene(sc[n % len(sc)], nthreads=cores)
+            n += 1
+            if time.perf_counter() - t0 > 5.0:
+                break
+        t_all += time.perf_counter() - t0
+    rate = n / t_all
+    unit = "scenes/s" if args.config == 3 else "requests/s"
+    line = {
+        "impl": "reference", "metric": unit, "value": rate, "unit": unit, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_all / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "batch of %d scenes (config 3 scene mix)" % len(sc), "config_index": args.config},
+        "cpu_baseline": {"value": rate, "unit": unit, "cores": cores, "kind": "port",
+                         "sample": f"the first {n} scenes of the mix in {t_all:.1f} s, row bands over "
+                                   f"{cores} threads (the reference crate is Rust; no toolchain here)"},
+        "e2e": {"value": rate, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    if args.config in (3, 4):
+        return run_reference_scenes(args)
     scene = make_scene(args.config)
     import oracle
     cores = os.cpu_count() or 1
