@@ -28,14 +28,19 @@ def channel_diff(a, b):
     return d
 
 
-def assert_parity(scene, tile=0, log=True, nthreads=1, colour_lsb=0):
+def assert_parity(scene, tile=0, log=True, nthreads=1, colour_lsb=0, log_capacity=0):
     """Coverage (fragment log), depth-passed masks, per-sample depth and colour bit-exact;
-    resolved ARGB within colour_lsb per channel (0 = bit-exact, the expected result)."""
-    cap = 4 * scenes.scene_triangles(scene) + 4 * scene["width"] * scene["height"] if log else 0
+    resolved ARGB within colour_lsb per channel (0 = bit-exact, the expected result).
+    A log that reaches its capacity fails the test: both sides drop the rows past it, and the
+    GPU's rows arrive in no fixed order, so a full log compares different subsets."""
+    cap = 0
+    if log:
+        cap = log_capacity or 4 * scenes.scene_triangles(scene) + 4 * scene["width"] * scene["height"]
     ga, gd, gc, gs, gst, glog = gpu_render(scene, tile=tile, log_capacity=cap)
     oa, od, oc, os_, ost, olog = oracle.render_scene(scene, nthreads=nthreads if not log else 1,
                                                      log_capacity=cap)
     if log:
+        assert len(olog) < cap and len(glog) < cap, f"fragment log full at {cap} rows: raise log_capacity"
         gl, ol = sort_log(glog), sort_log(olog)
         assert gl.shape == ol.shape, (gl.shape, ol.shape)
         bad = np.nonzero((gl != ol).any(1))[0]
