@@ -63,9 +63,9 @@ __device__ __forceinline__ uint32_t bin_entry(uint32_t tri, bool clipped, unsign
     const uint32_t ox = tx * ts, oy = ty * ts, rsh = __ffs(rs) - 1, nsx = ts >> rsh;
     const uint32_t sx0 = (max(px0, ox) - ox) >> rsh, sx1 = (min(px1, ox + ts - 1) - ox) >> rsh;
     const uint32_t sy0 = (max(py0, oy) - oy) >> rsh, sy1 = (min(py1, oy + ts - 1) - oy) >> rsh;
+    const uint32_t xm = (2u << sx1) - (1u << sx0);  // quadrant columns sx0 .. sx1
     uint32_t m = 0;
-    for (uint32_t sy = sy0; sy <= sy1; ++sy)
-        for (uint32_t sx = sx0; sx <= sx1; ++sx) m |= 1u << (sy * nsx + sx);
+    for (uint32_t sy = sy0; sy <= sy1; ++sy) m |= xm << (sy * nsx);
     return head | m;
 }
 
@@ -442,6 +442,7 @@ constexpr int kPairsPerBatch = 512;  // (triangle, tile) pairs ranked per batch
 constexpr uint32_t kBigTri = 32;     // triangles over more tiles are binned alone, tile-parallel
 constexpr int kHashSlots = 1024;     // open-addressing table over tile ids, load <= 0.5
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+constexpr unsigned long long kRectClippedBit = 1ull << 63;  // pixel boxes stay below 2^15
 
 __device__ __forceinline__ uint32_t hash_slot(uint32_t t) {
     return (t * 2654435761u) >> (32 - 10);
@@ -464,9 +465,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     __shared__ uint32_t pxy[kPairsPerBatch];  // tile x | tile y << 16
     __shared__ uint16_t pslot[kPairsPerBatch], prank[kPairsPerBatch];
     __shared__ uint16_t ptri[kPairsPerBatch];
-    __shared__ unsigned long long trect[kScatterWindow];
-    __shared__ uint32_t tclip[kScatterWindow / 32];
-    __shared__ uint32_t nslots, take_s;
+    __shared__ unsigned long long trect[kScatterWindow];  // pixel box, bit 63: clipped
+    __shared__ uint32_t sbase[kHashSlots];  // per slot: the tile's position before the batch
+    __shared__ uint32_t nslots, take_s, npairs_s;
     __shared__ uint32_t tmp[33];
     if (*(volatile uint32_t*)s.status & ST_BIN_OVERFLOW) return;
     const ChunkDev ch = chunks[blockIdx.x];
@@ -502,25 +503,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             const uint32_t i = base + v;
             const bool live = i < ch.tri_count;
             r[j] = live ? s.tri_rect[gbase + i] : kRectEmpty;
-            const bool clipped = live && s.tri_aux[gbase + i] != kNone;
+            const bool clipped = live && r[j] != kRectEmpty && s.tri_aux[gbase + i] != kNone;
             n[j] = rect_tiles(r[j], ts);
-            trect[v] = r[j];
-            const uint32_t cb = __ballot_sync(0xFFFFFFFFu, clipped);
-            // bit v of tclip: interleave the two ballots back into window order
-            if (lane == 0) {
-                uint32_t lo = 0, hi = 0;
-                for (int q = 0; q < 16; ++q) {
-                    lo |= ((cb >> q) & 1u) << (2 * q + j);
-                    hi |= ((cb >> (q + 16)) & 1u) << (2 * q + j);
-                }
-                if (j == 0) {
-                    tclip[warp * 2] = lo;
-                    tclip[warp * 2 + 1] = hi;
-                } else {
-                    tclip[warp * 2] |= lo;
-                    tclip[warp * 2 + 1] |= hi;
-                }
-            }
+            trect[v] = clipped ? (r[j] | kRectClippedBit) : r[j];
             mine += n[j];
         }
         if (threadIdx.x == 0) take_s = kScatterWindow;
@@ -544,8 +529,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
         if (take == 0) {
             // a single triangle over more than kBigTri tiles: its tiles are distinct, each
             // takes the next position
-            const unsigned long long r0 = trect[0];
-            const bool c0 = tclip[0] & 1u;
+            const bool c0 = (trect[0] & kRectClippedBit) != 0;
+            const unsigned long long r0 = trect[0] & ~kRectClippedBit;
             uint32_t x0, y0, x1, y1;
             tile_rect(r0, ts, x0, y0, x1, y1);
             const uint32_t w = x1 - x0 + 1, n0 = rect_tiles(r0, ts);
@@ -594,7 +579,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                 const uint32_t j = o < n0 ? 0u : 1u, k = o < n0 ? o : o - n0;
                 v = (warp * 32 + src) * kScatterTriPerThread + j;
                 uint32_t x0, y0, x1, y1;
-                tile_rect(trect[v], ts, x0, y0, x1, y1);
+                tile_rect(trect[v] & ~kRectClippedBit, ts, x0, y0, x1, y1);
                 const uint32_t w = x1 - x0 + 1;
                 const uint32_t ky = k < w ? 0u : k / w;
                 const uint32_t ttx = x0 + (k - ky * w), tty = y0 + ky;
@@ -629,17 +614,6 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                 ptri[bp] = (uint16_t)v;
             }
         }
-        __syncthreads();
-        // ---- positions: running offset + earlier warps' counts + rank in the warp
-        // first meeting of a tile in this chunk: load its running offset
-        for (uint32_t j = threadIdx.x; j < nslots; j += blockDim.x) {
-            const uint32_t t = hkey[slot_list[j]];
-            if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
-                run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
-                atomicOr(&valid[t >> 5], 1u << (t & 31u));
-            }
-        }
-        uint32_t npairs = 0;  // pairs of the batch: those of the taken triangles
         {
             const uint32_t t_last = take - 1;  // its thread holds the end of the batch's pairs
             if (threadIdx.x == t_last / kScatterTriPerThread) {
@@ -647,35 +621,49 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 #pragma unroll
                 for (int j = 0; j < kScatterTriPerThread; ++j)
                     if (threadIdx.x * kScatterTriPerThread + j < take) e += n[j];
-                tmp[0] = e;
+                npairs_s = e;
             }
         }
         __syncthreads();
-        npairs = tmp[0];
-        for (uint32_t bp = threadIdx.x; bp < npairs; bp += blockDim.x) {
-            const uint32_t xy = pxy[bp], slot = pslot[bp], v = ptri[bp];
-            const uint32_t ttx = xy & 0xFFFFu, tty = xy >> 16, t = tty * tx + ttx;
-            const uint32_t pw = v / (32 * kScatterTriPerThread);
-            uint32_t before = prank[bp];
-            for (uint32_t w2 = 0; w2 < pw; ++w2) before += wcnt[slot][w2];
-            const uint32_t pos = run_off[t] + before;
-            const bool clipped = (tclip[v >> 5] >> (v & 31u)) & 1u;
-            if (pos < cap) bins[pos] = bin_entry(fbase + base + v, clipped, trect[v], ttx, tty, ts);
-        }
-        __syncthreads();
-        const uint32_t ns = nslots;
+        // ---- per tile of the batch: its position before the batch (loaded from the chunk's
+        // offsets when the chunk first meets the tile), the warps' counts turned into
+        // exclusive prefixes, and the position advanced past the batch
+        const uint32_t ns = nslots, npairs = npairs_s;
         for (uint32_t j = threadIdx.x; j < ns; j += blockDim.x) {
-            const uint32_t h = slot_list[j];
-            uint32_t cnt = 0;
+            const uint32_t h = slot_list[j], t = hkey[h];
+            if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
+                run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
+                atomicOr(&valid[t >> 5], 1u << (t & 31u));
+            }
+            const uint32_t b = run_off[t];
+            uint32_t tot = 0;
 #pragma unroll
             for (int w2 = 0; w2 < kScatterWarps; ++w2) {
-                cnt += wcnt[h][w2];
-                wcnt[h][w2] = 0;
+                const uint32_t c = wcnt[h][w2];
+                wcnt[h][w2] = (uint16_t)tot;
+                tot += c;
             }
-            run_off[hkey[h]] += cnt;
-            hkey[h] = kHashEmpty;
+            sbase[h] = b;
+            run_off[t] = b + tot;
         }
         __syncthreads();
+        // ---- positions: the tile's position + earlier warps' counts + rank in the warp
+        for (uint32_t bp = threadIdx.x; bp < npairs; bp += blockDim.x) {
+            const uint32_t xy = pxy[bp], slot = pslot[bp], v = ptri[bp];
+            const uint32_t pw = v / (32 * kScatterTriPerThread);
+            const uint32_t pos = sbase[slot] + wcnt[slot][pw] + prank[bp];
+            const unsigned long long rv = trect[v];
+            const bool clipped = (rv & kRectClippedBit) != 0;
+            if (pos < cap)
+                bins[pos] = bin_entry(fbase + base + v, clipped, rv & ~kRectClippedBit, xy & 0xFFFFu, xy >> 16, ts);
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < ns; j += blockDim.x) {
+            const uint32_t h = slot_list[j];
+#pragma unroll
+            for (int w2 = 0; w2 < kScatterWarps; ++w2) wcnt[h][w2] = 0;
+            hkey[h] = kHashEmpty;
+        }
         if (threadIdx.x == 0) nslots = 0;
         __syncthreads();
         base += take;
