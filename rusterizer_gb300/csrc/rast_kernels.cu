@@ -675,6 +675,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 constexpr int kRasterThreads = 256;
 constexpr int kRasterWarps = kRasterThreads / 32;
 constexpr int kEmptyRun = 8;  // bins without entries taken per queue update
+constexpr uint32_t kTrimMin = 4;  // shortest box line that line_span trims
 
 // A raster CTA owns one TS x TS tile: a whole bin (bin edge == TS) or one quadrant of a bin
 // twice as wide. Bin entries carry, in their low 4 bits, the quadrants the triangle's pixel box
@@ -753,17 +754,31 @@ __device__ __forceinline__ void item_normal(const RasterSmem<S, TS>& sm, uint32_
     ny = vx;
 }
 
+// Room added to edge k's value at a pixel centre so that it bounds the computed edge value at
+// every sample of the pixel: s_k + m_k, derived at line_span.
+template <int S>
+__device__ __forceinline__ float edge_room(float nx, float ny, float Px, float Py) {
+    const float sk = S == 1 ? 0.0f : 0.125f * fmaxf(fabsf(nx - 3.0f * ny), fabsf(3.0f * nx + ny));
+    return sk + 1e-6f * (fabsf(nx) * (fabsf(Px) + 16400.0f) + fabsf(ny) * (fabsf(Py) + 16400.0f)) + 1e-37f;
+}
+
 // The pixels of one line of an item's box that can hold a covered sample: line lc (a tile-local
 // row in mode 0, a column in mode 1), candidates [a0, a1) along it, trimmed in place. A pixel is
 // dropped only where some edge k is negative at every sample with room to spare: with E_k the
 // edge function in exact arithmetic over the stored f32 normal and point, the computed
 // edge_eval value differs from E_k by at most 3 * 2^-24 * (|nx| |x - Px| + |ny| |y - Py|)
 // (two subtractions, two products and one sum, each correctly rounded; the leading 0 + is
-// exact), so E_k(centre) + 3/8 (|nx| + |ny|) + m_k < 0, m_k = 1e-6 (|nx| (|Px| + 16400) +
-// |ny| (|Py| + 16400)) + 1e-37, makes every sample's computed value negative, and the edge
-// test fails whatever the tie rule (screen coordinates stay below 16400). The threshold along
-// the line is computed in f32 and widened by a pixel on each side. Non-finite points are not
-// trimmed.
+// exact). E_k is linear, so over the pixel's samples it is at most E_k(centre) + s_k, s_k the
+// largest of nx ox + ny oy over the sample offsets (ox, oy) from the centre: for the 4-sample
+// pattern (1/8, -3/8), (3/8, 1/8) and their negatives, s_k = max(|nx - 3 ny|, |3 nx + ny|) / 8;
+// 0 for the single centre sample. So E_k(centre) + s_k + m_k < 0, m_k = 1e-6 (|nx| (|Px| +
+// 16400) + |ny| (|Py| + 16400)) + 1e-37, makes every sample's computed value negative, and the
+// edge test fails whatever the tie rule (screen coordinates stay below 16400; m_k also covers
+// the f32 rounding of s_k and of the line offset below). Along the line the bound is linear in
+// the pixel index, so the pixels that keep it are an interval [ceil(t), ...) or (..., t]; t is
+// computed in f32 to within 0.03 pixel whenever it falls near the tile (|pal - gk / nal| below
+// 2^16; farther out only its sign matters), and the interval is widened by 1/8 pixel.
+// Non-finite points are not trimmed.
 template <int S, int TS>
 __device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t it, uint32_t mode, uint32_t lc,
                                           uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
@@ -773,7 +788,6 @@ __device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t 
 #pragma unroll
     for (int k = 0; k < 3; ++k) finite = finite && isfinite(px[k]) && isfinite(py[k]);
     if (!finite) return;
-    const float rs = S == 1 ? 0.0f : 0.375f;
     // line centre across, and the pixel-centre origin along the line (global coordinates)
     const float cacross = (float)((mode == 0 ? Y0 : X0) + lc) + 0.5f;
     const float oalong = (float)(mode == 0 ? X0 : Y0) + 0.5f;
@@ -782,9 +796,7 @@ __device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t 
     for (int k = 0; k < 3; ++k) {
         const int n = k == 2 ? 0 : k + 1;
         const float nx = -(py[n] - py[k]), ny = px[n] - px[k];
-        const float R = rs * (fabsf(nx) + fabsf(ny)) +
-                        1e-6f * (fabsf(nx) * (fabsf(px[k]) + 16400.0f) + fabsf(ny) * (fabsf(py[k]) + 16400.0f)) +
-                        1e-37f;
+        const float R = edge_room<S>(nx, ny, px[k], py[k]);
         const float nal = mode == 0 ? nx : ny, nac = mode == 0 ? ny : nx;
         const float pal = mode == 0 ? px[k] : py[k], pac = mode == 0 ? py[k] : px[k];
         const float gk = nac * (cacross - pac) + R;  // E_k + R = nal * (c_along - pal) + gk
@@ -794,12 +806,11 @@ __device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t 
             continue;
         }
         // E_k + R >= 0  <=>  nal * (oalong + x - pal) >= -gk
-        const float t = pal - __fdividef(gk, nal) - oalong;  // widened below: 2-ulp division is enough
+        const float t = pal - __fdividef(gk, nal) - oalong;  // 2-ulp division is enough
         if (!isfinite(t)) continue;
         const float tc = fminf(fmaxf(t, -8.0f), (float)TS + 8.0f);
-        const int ti = (int)floorf(tc);
-        if (nal > 0.0f) lo = max(lo, ti - 1);
-        else hi = min(hi, ti + 2);
+        if (nal > 0.0f) lo = max(lo, (int)ceilf(tc - 0.125f));
+        else hi = min(hi, (int)floorf(tc + 0.125f) + 1);
     }
     if (hi < lo) hi = lo;
     a0 = (uint32_t)lo;
@@ -1256,8 +1267,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 const uint32_t first = l0 + ((warp + kRasterWarps - (l0 % kRasterWarps)) % kRasterWarps);
                 const uint32_t nlines = first < l1 ? (l1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
                 uint32_t s1 = b0, e1 = b1, s2 = b0, e2 = b1;
-                // lines shorter than 4 pixels are cheaper to test whole than to trim
-                const uint32_t ntrim = b1 - b0 >= 4 ? nlines : 0u;
+                // lines shorter than kTrimMin pixels are cheaper to test whole than to trim
+                const uint32_t ntrim = b1 - b0 >= kTrimMin ? nlines : 0u;
 #pragma unroll 1
                 for (uint32_t ln = 0; ln < ntrim; ++ln) {
                     uint32_t a0 = b0, a1 = b1;
