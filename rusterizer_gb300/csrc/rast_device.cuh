@@ -214,6 +214,30 @@ __device__ __forceinline__ float interp_depth(float e1, float e2, float inv, flo
     return b0 * z0 + b1 * z1 + b2 * z2;
 }
 
+// clamp01 that returns a NaN as a NaN of unspecified payload and may return +0.0 for -0.0
+// (max.NaN / min.NaN: two instructions).
+__device__ __forceinline__ float clamp01_nan(float x) {
+    float r;
+    asm("max.NaN.f32 %0, %1, 0f00000000;" : "=f"(r) : "f"(x));
+    asm("min.NaN.f32 %0, %1, 0f3F800000;" : "=f"(r) : "f"(r));
+    return r;
+}
+
+// interp_depth for edge values that may carry either sign of zero (edge_eval_test), with
+// clamp01_nan. The depth comes out bit for bit as interp_depth's over edge_eval, except for
+// the payload of a NaN (a NaN depth never passes the depth test, and a shader that reads it
+// saturates it to 0): flipping the sign of a zero b0 or b1 flips only the sign of a zero
+// product b * z, and the sum can then only change from +0 to -0 when another product is -0
+// too, which needs a corner depth of -0 -- the viewport's final + zmin makes every screen
+// depth +0 rather than -0; b2 = clamp01((1 - b0) - b1) is never -0.
+__device__ __forceinline__ float interp_depth_fast(float e1, float e2, float inv, float z0, float z1,
+                                                   float z2) {
+    const float b0 = clamp01_nan(e1 * inv);
+    const float b1 = clamp01_nan(e2 * inv);
+    const float b2 = clamp01_nan(1.0f - b0 - b1);
+    return b0 * z0 + b1 * z1 + b2 * z2;
+}
+
 // RGSS_SAMPLE_PATTERN (src/rasterizer/mod.rs:109-114); 1 sample = pixel centre (extension).
 template <int S>
 __device__ __forceinline__ float sample_dx(int i) {

@@ -1333,11 +1333,11 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                     for (int k = 0; k < S; ++k) {
                         const float xs = fx + sample_dx<S>(k), ys = fy + sample_dy<S>(k);
                         const float e0 = edge_eval_test(n0x, n0y, p0x, p0y, xs, ys);
-                        const float e1 = edge_eval(n1x, n1y, p1x, p1y, xs, ys);
-                        const float e2 = edge_eval(n2x, n2y, p2x, p2y, xs, ys);
+                        const float e1 = edge_eval_test(n1x, n1y, p1x, p1y, xs, ys);
+                        const float e2 = edge_eval_test(n2x, n2y, p2x, p2y, xs, ys);
                         // branch-free: every sample's depth is computed, the covered ones kept
                         const bool in = edge_pass_t(e0, t0) & edge_pass_t(e1, t1) & edge_pass_t(e2, t2);
-                        const float zk = interp_depth(e1, e2, inv, z0, z1, z2);
+                        const float zk = interp_depth_fast(e1, e2, inv, z0, z1, z2);
                         cov |= (uint32_t)in << k;
                         z[k] = in ? zk : 0.0f;
                     }
