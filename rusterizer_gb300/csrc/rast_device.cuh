@@ -205,15 +205,6 @@ __device__ __forceinline__ float edge_eval_test(float nx, float ny, float px, fl
 __device__ __forceinline__ bool edge_tie(float nx, float ny) { return (nx > 0.0f) | (!(nx < 0.0f) & (ny < 0.0f)); }
 __device__ __forceinline__ bool edge_pass_t(float e, bool tie) { return (e > 0.0f) | (!(e < 0.0f) & tie); }
 
-// RasterizerTriangle::fragment's interpolate_depth (src/rasterizer/mod.rs:226-236)
-__device__ __forceinline__ float interp_depth(float e1, float e2, float inv, float z0, float z1,
-                                              float z2) {
-    float b0 = clamp01(e1 * inv);
-    float b1 = clamp01(e2 * inv);
-    float b2 = clamp01(1.0f - b0 - b1);
-    return b0 * z0 + b1 * z1 + b2 * z2;
-}
-
 // clamp01 that returns a NaN as a NaN of unspecified payload and may return +0.0 for -0.0
 // (max.NaN / min.NaN: two instructions).
 __device__ __forceinline__ float clamp01_nan(float x) {
@@ -223,13 +214,15 @@ __device__ __forceinline__ float clamp01_nan(float x) {
     return r;
 }
 
-// interp_depth for edge values that may carry either sign of zero (edge_eval_test), with
-// clamp01_nan. The depth comes out bit for bit as interp_depth's over edge_eval, except for
-// the payload of a NaN (a NaN depth never passes the depth test, and a shader that reads it
-// saturates it to 0): flipping the sign of a zero b0 or b1 flips only the sign of a zero
-// product b * z, and the sum can then only change from +0 to -0 when another product is -0
-// too, which needs a corner depth of -0 -- the viewport's final + zmin makes every screen
-// depth +0 rather than -0; b2 = clamp01((1 - b0) - b1) is never -0.
+// RasterizerTriangle::fragment's interpolate_depth (src/rasterizer/mod.rs:226-236):
+// b0 = clamp(e1 inv), b1 = clamp(e2 inv), b2 = clamp((1 - b0) - b1), z = (b0 z0 + b1 z1) +
+// b2 z2 with inv = 1 / triangle_2x_area, here over edge values that may carry either sign of zero (edge_eval_test) and with
+// clamp01_nan. The depth comes out bit for bit as the reference's (edge values with the
+// leading 0 +, clamp01), except for the payload of a NaN (a NaN depth never passes the depth
+// test, and a shader that reads it saturates it to 0): flipping the sign of a zero b0 or b1
+// flips only the sign of a zero product b * z, and the sum can then only change from +0 to
+// -0 when another product is -0 too, which needs a corner depth of -0 -- the viewport's final
+// + zmin makes every screen depth +0 rather than -0; b2 = clamp01((1 - b0) - b1) is never -0.
 __device__ __forceinline__ float interp_depth_fast(float e1, float e2, float inv, float z0, float z1,
                                                    float z2) {
     const float b0 = clamp01_nan(e1 * inv);

@@ -1709,17 +1709,18 @@ __global__ void k_kat(int op, const unsigned char* __restrict__ in, unsigned cha
                 for (int v = 0; v < 3; ++v) sv[v].w = fi[11 + v];
             TriSetup t;
             tri_setup(t, sv);
+            // the raster kernel's coverage and sample-depth arithmetic
             uint32_t cov = 0;
             float d[4] = {0, 0, 0, 0};
             for (int q = 0; q < 4; ++q) {
                 const float xs = (float)x + sample_dx<4>(q), ys = (float)y + sample_dy<4>(q);
                 float e[3];
-                for (int k = 0; k < 3; ++k) e[k] = edge_eval(t.nx[k], t.ny[k], t.px[k], t.py[k], xs, ys);
+                for (int k = 0; k < 3; ++k) e[k] = edge_eval_test(t.nx[k], t.ny[k], t.px[k], t.py[k], xs, ys);
                 bool in3 = true;
                 for (int k = 0; k < 3; ++k) in3 = in3 && edge_pass_t(e[k], edge_tie(t.nx[k], t.ny[k]));
                 if (in3) {
                     cov |= 1u << q;
-                    d[q] = interp_depth(e[1], e[2], t.inv_area, t.z[0], t.z[1], t.z[2]);
+                    d[q] = interp_depth_fast(e[1], e[2], t.inv_area, t.z[0], t.z[1], t.z[2]);
                 }
             }
             if (op == 2) {

@@ -44,11 +44,11 @@ __host__ __device__
 constexpr int raster_edge(int ts) { return ts > 16 ? 16 : ts; }
 
 // Triangles per binning chunk (one CTA of the count and scatter kernels; one row of per-tile
-// counts): about 900 chunks for large meshes, a multiple of 256 in [512, 8192].
+// counts): about 900 chunks for large meshes, a multiple of 256 in [256, 8192].
 inline uint32_t chunk_size_for(uint32_t ntris) {
     uint32_t c = (ntris + 899u) / 900u;
     c = (c + 255u) & ~255u;
-    return c < 512u ? 512u : (c > 8192u ? 8192u : c);
+    return c < 256u ? 256u : (c > 8192u ? 8192u : c);
 }
 
 enum StatusBits : uint32_t {
