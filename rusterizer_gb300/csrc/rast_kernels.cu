@@ -716,6 +716,7 @@ struct RasterSmem {
     int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
     uint32_t tmp[40];
     uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split mode
+    uint32_t zmaxw[kRasterWarps];  // per warp: largest stored depth of its share of the tile
 
 };
 
@@ -817,6 +818,27 @@ __device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t 
     a1 = (uint32_t)hi;
 }
 
+// Order-preserving map of floats to unsigned integers (NaN above +inf) and back.
+__device__ __forceinline__ uint32_t float_to_ordered(float x) {
+    const uint32_t b = __float_as_uint(x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// True when no sample of the triangle with screen depths z0..z2 can pass the strict depth
+// test against a tile whose stored depths are all <= ztile. A sample depth is (b0 z0 + b1 z1)
+// + b2 z2 with clamped b0, b1 in [0, 1] and b2 = clamp((1 - b0) - b1): a convex combination,
+// or with b2 = 0 a combination with b0 + b1 >= 1, so for depths >= 0 it is at least
+// min(z0, z1, z2) up to the rounding of the products and sums (well below 2^-20 relative).
+// Never true with a negative or NaN corner depth or a NaN ztile.
+__device__ __forceinline__ bool depth_cull(float z0, float z1, float z2, float ztile) {
+    const float zmin = fminf(fminf(z0, z1), z2);
+    const bool ok = z0 >= 0.0f && z1 >= 0.0f && z2 >= 0.0f;  // false for NaN
+    return ok && zmin * (1.0f - 0x1p-20f) >= ztile;
+}
+
 // Stages the items of one bin entry (one triangle, or the fan of its clipped polygon) at
 // positions first.. of the batch: screen points, depths, w, attributes, 1 / 2x area and the
 // tile-local pixel box, and adds the box to the batch's row and column work.
@@ -824,7 +846,7 @@ template <int S, int TS>
 __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDev& f,
                                             const DrawDev* __restrict__ draws, const Scratch& s,
                                             uint32_t g, uint32_t aux, uint32_t nitems, uint32_t first,
-                                            uint32_t X0, uint32_t Y0) {
+                                            uint32_t X0, uint32_t Y0, float ztile) {
     const uint32_t di = find_draw(draws, f, g);
     const DrawDev& d = draws[di];
     const int fs = d.fs;
@@ -870,7 +892,10 @@ __device__ __forceinline__ void stage_entry(RasterSmem<S, TS>& sm, const FrameDe
         pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
         const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
         const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
-        const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1;
+        // hidden: no sample depth can get below the largest depth stored in the tile
+        // (depth_cull), so the strict depth test (mod.rs:363-378) fails everywhere
+        const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1 &&
+                              !depth_cull(sv[0].z, sv[1].z, sv[2].z, ztile);
         uint32_t r = 0;
         if (nonempty) {
             const uint32_t lx0 = cx0 - X0, ly0 = cy0 - Y0, lx1 = cx1 - X0, ly1 = cy1 - Y0;
@@ -1179,6 +1204,18 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             sm.rowd[threadIdx.x] = 0;
             sm.cold[threadIdx.x] = 0;
         }
+        // largest depth stored in the tile before this batch, for depth_cull: the clear depth
+        // for the unit's first batch; else reduced here and combined after the scan's barriers.
+        // NaN (no culling) while the fragment log records depth-failed fragments too.
+        float zt = s.log ? __int_as_float(0x7FC00000) : f.clear_depth;
+        bool zt_ready = s.log || pos == 0;
+        if (!zt_ready) {
+            uint32_t zm = 0;
+            for (uint32_t i = threadIdx.x; i < (uint32_t)(C::NPIX * S); i += blockDim.x)
+                zm = max(zm, float_to_ordered(sm.zb[i]));
+            zm = __reduce_max_sync(0xFFFFFFFFu, zm);
+            if (lane == 0) sm.zmaxw[warp] = zm;
+        }
         uint32_t nit = 0;
         while (pos < nent) {
             const uint32_t e = pos + threadIdx.x;
@@ -1201,7 +1238,16 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             const bool part = (e < nent) && (nit + iex + nitems <= (uint32_t)C::IC);
             const uint32_t take = __syncthreads_count(part);
             if (part && threadIdx.x == take - 1) sm.misc[1] = nit + iex + nitems;
-            if (part && nitems) stage_entry<S, TS>(sm, f, draws, s, g, aux, nitems, nit + iex, X0, Y0);
+            if (part && nitems) {
+                if (!zt_ready) {
+                    uint32_t zm = sm.zmaxw[0];
+#pragma unroll
+                    for (int w = 1; w < kRasterWarps; ++w) zm = max(zm, sm.zmaxw[w]);
+                    zt = ordered_to_float(zm);
+                    zt_ready = true;
+                }
+                stage_entry<S, TS>(sm, f, draws, s, g, aux, nitems, nit + iex, X0, Y0, zt);
+            }
             __syncthreads();
             nit = sm.misc[1];
             const uint32_t window = min(nent - pos, (uint32_t)kRasterThreads);

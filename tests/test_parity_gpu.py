@@ -123,6 +123,16 @@ def test_texture_wrap_and_out_of_bounds_reads():
     assert gs["texture_oob"] > 0
 
 
+@pytest.mark.parametrize("msaa,tile", [(4, 16), (1, 32), (4, 8)])
+def test_high_depth_complexity(msaa, tile):
+    """Tens of thousands of triangles over a small frame (hundreds of layers per pixel), without
+    the fragment log, so that whole triangles are skipped where the tile's stored depths are
+    already nearer than every depth they can produce: samples, image and counts stay exact."""
+    s = scenes.small_soup(31 + msaa + tile, ntris=30000, width=96, height=80, msaa=msaa)
+    ga, gs = assert_parity(s, tile=tile, log=False, nthreads=8)
+    assert gs["fs_invocations"] > 0
+
+
 def test_config1_full_size():
     assert_parity(scenes.config1(), log=False, nthreads=8)
 
