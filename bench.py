@@ -31,7 +31,16 @@ sys.path.insert(0, ROOT)
 CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
            1: "triangle soup 100k tris 1920x1080 4xMSAA",
            2: "heightfield 2M tris 3840x2160 4xMSAA"}
-LAUNCHES_PER_FRAME = 8  # vertex, bin count, clip, column scan, tile scan, scatter, tile order, raster
+MAX_TILES_PER_FRAME = 16384  # the library's per-frame bin limit (rast_types.h kMaxTilesPerFrame)
+
+
+def launches_per_frame(width, height, tile=0):
+    """Kernels per plain frame: vertex, bin count, clip, column scan, tile scan, scatter, tile
+    order, raster, plus the quadrant split when the frame uses 32-pixel bins (the library picks
+    16-pixel bins unless a frame would have more than MAX_TILES_PER_FRAME of them)."""
+    if tile not in (8, 16, 32):
+        tile = 16 if -(-width // 16) * -(-height // 16) <= MAX_TILES_PER_FRAME else 32
+    return 9 if tile == 32 else 8
 
 
 def make_scene(cfg):
@@ -387,7 +396,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": W * H * 4, "host_threads": 2,
                     "one_thread_value": e2e_serial},
-            "gpu_launches": LAUNCHES_PER_FRAME * args.steps,
+            "gpu_launches": launches_per_frame(W, H, args.tile) * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
