@@ -32,14 +32,19 @@ CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
            1: "triangle soup 100k tris 1920x1080 4xMSAA",
            2: "heightfield 2M tris 3840x2160 4xMSAA"}
 MAX_TILES_PER_FRAME = 16384  # the library's per-frame bin limit (rast_types.h kMaxTilesPerFrame)
+AUTO_BIG_BIN_TRIS = 8192  # from this many triangles the library picks 32-pixel bins (rast_internal.h)
 
 
-def launches_per_frame(width, height, tile=0):
+def launches_per_frame(width, height, ntris, tile=0):
     """Kernels per plain frame: vertex, bin count, clip, column scan, tile scan, scatter, tile
-    order, raster, plus the quadrant split when the frame uses 32-pixel bins (the library picks
-    16-pixel bins unless a frame would have more than MAX_TILES_PER_FRAME of them)."""
-    if tile not in (8, 16, 32):
-        tile = 16 if -(-width // 16) * -(-height // 16) <= MAX_TILES_PER_FRAME else 32
+    order, raster, plus the quadrant split when the frame uses 32-pixel bins (the library's
+    automatic choice: 32-pixel bins for frames of AUTO_BIG_BIN_TRIS triangles or more, else 16,
+    either one when the other would exceed MAX_TILES_PER_FRAME bins)."""
+    def fits(t):
+        return -(-width // t) * -(-height // t) <= MAX_TILES_PER_FRAME
+    if not (tile in (8, 16, 32) and fits(tile)):
+        order = (32, 16) if ntris >= AUTO_BIG_BIN_TRIS else (16, 32)
+        tile = next(t for t in order if fits(t))
     return 9 if tile == 32 else 8
 
 
@@ -396,7 +401,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": W * H * 4, "host_threads": 2,
                     "one_thread_value": e2e_serial},
-            "gpu_launches": launches_per_frame(W, H, args.tile) * args.steps,
+            "gpu_launches": launches_per_frame(W, H, scenes.scene_triangles(scene), args.tile) * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

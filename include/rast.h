@@ -57,7 +57,8 @@ void rast_destroy(rast_ctx* ctx);
 
 /* Depth clear value; the reference uses f32::MAX (src/rasterizer/buffers.rs:6). */
 rast_status rast_set_clear_depth(rast_ctx* ctx, float depth);
-/* Screen tile edge in pixels (8, 16 or 32); 0 selects automatically. */
+/* Screen tile edge in pixels (8, 16 or 32); 0 selects automatically: 32 for frames of 8192
+ * triangles or more, else 16 (either one when the other would exceed 16384 tiles). */
 rast_status rast_set_tile_size(rast_ctx* ctx, int tile);
 
 /* Upload a mesh (Mesh{vertices, indices, attributes}, src/mesh.rs:5-12) so that it stays

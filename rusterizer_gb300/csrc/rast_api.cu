@@ -36,13 +36,14 @@ void mat4_mul(const float* a, const float* b, float* out) {
     std::memcpy(out, r, sizeof(r));
 }
 
-int choose_tile(int w, int h, int msaa, int req) {
+int choose_tile(int w, int h, int msaa, int req, uint64_t ntris) {
     if (req == 8 || req == 16 || req == 32) {
         long long n = (long long)((w + req - 1) / req) * ((h + req - 1) / req);
         if (n <= kMaxTilesPerFrame) return req;
     }
     (void)msaa;
-    for (int ts : {16, 32}) {
+    const bool big = ntris >= kAutoBigBinTris;
+    for (int ts : {big ? 32 : 16, big ? 16 : 32}) {
         long long n = (long long)((w + ts - 1) / ts) * ((h + ts - 1) / ts);
         if (n <= kMaxTilesPerFrame) return ts;
     }
@@ -468,7 +469,10 @@ rast_status rast_draw(rast_ctx* c, rast_mesh mesh, int vs_id, int fs_id) {
 
 static rast_status framebuffer_impl(rast_ctx* c, uint32_t* argb_out, bool sync) {
     if (!c) return RAST_INVALID_ARG;
-    const int ts = choose_tile(c->width, c->height, c->msaa, c->tile_req);
+    uint64_t ntris = 0;
+    for (const DrawJob& d : c->queue)
+        if (d.mesh_id < c->meshes.size() && c->meshes[d.mesh_id].live) ntris += c->meshes[d.mesh_id].ntris;
+    const int ts = choose_tile(c->width, c->height, c->msaa, c->tile_req, ntris);
     if (!ts) return RAST_INVALID_ARG;
     const size_t npx = (size_t)c->width * (size_t)c->height;
     bool dev_out = false;

@@ -32,7 +32,8 @@ bool is_device_ptr(const void* p) {
 int scene_tile(const rast_ctx* c, const rast_scene& s) {
     int req = s.tile;
     if (req == 0) req = c->tuned_tile[s.msaa == 4 ? 1 : 0];
-    return choose_tile(s.width, s.height, s.msaa, req);
+    const bool mesh_ok = s.mesh < c->meshes.size() && c->meshes[s.mesh].live;
+    return choose_tile(s.width, s.height, s.msaa, req, mesh_ok ? c->meshes[s.mesh].ntris : 0u);
 }
 
 // Validates the scenes and turns them into frame jobs. Host outputs (when allowed) are

@@ -244,7 +244,12 @@ struct Engine {
 };
 
 void mat4_mul(const float* a, const float* b, float* out);
-int choose_tile(int w, int h, int msaa, int req);
+// Bin edge for a frame: the requested 8, 16 or 32 when the frame's bin count fits, else
+// automatic: 32-pixel bins from kAutoBigBinTris triangles on (the binning work grows with
+// chunks x bins, and quadrant rastering keeps 16-pixel raster tiles), 16-pixel bins below.
+// 0 when no bin size fits.
+constexpr uint64_t kAutoBigBinTris = 8192;
+int choose_tile(int w, int h, int msaa, int req, uint64_t ntris);
 rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs);
 
 }  // namespace rast

@@ -91,7 +91,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
     if ((nverts && (!d_pos || !d_uv)) || (ntris && !d_idx)) return RAST_INVALID_ARG;
     if (fs_id == RAST_FS_TEXTURE && (!d_tex || tex_w < 1 || tex_h < 1)) return RAST_INVALID_ARG;
     if (nverts > kNoAllocMaxVerts || ntris > kNoAllocMaxTris) return RAST_INVALID_ARG;
-    const int ts = choose_tile(width, height, msaa, tile);
+    const int ts = choose_tile(width, height, msaa, tile, ntris);
     if (!ts) return RAST_INVALID_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 

@@ -86,7 +86,8 @@ struct rast_server {
 
     int tile_of(const rast_scene& s) const {
         int req = s.tile ? s.tile : ctx->tuned_tile[s.msaa == 4 ? 1 : 0];
-        return choose_tile(s.width, s.height, s.msaa, req);
+        const bool mesh_ok = s.mesh < ctx->meshes.size() && ctx->meshes[s.mesh].live;
+        return choose_tile(s.width, s.height, s.msaa, req, mesh_ok ? ctx->meshes[s.mesh].ntris : 0u);
     }
 
     uint64_t hint_of(const rast_scene& s, int ts) const {
