@@ -1664,7 +1664,9 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    const uint32_t grid = a.nchunks < (uint32_t)(4 * sms) ? a.nchunks : (uint32_t)(4 * sms);
+    // up to four resident CTAs per SM (57 registers a thread), 32 warps per chunk: a frame of
+    // a few chunks spreads its straddlers over every SM, a tiny frame launches a few CTAs
+    const uint32_t grid = a.nchunks < (uint32_t)sms ? 4u * a.nchunks : (uint32_t)(4 * sms);
     k_clip<<<grid, 256, 0, a.stream>>>(a.draws, a.frames, a.scratch);
     return cudaGetLastError();
 }
