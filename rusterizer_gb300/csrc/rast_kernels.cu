@@ -73,6 +73,7 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
 
 // Block-wide exclusive scan of one u32 per thread (blockDim.x <= 1024). `tmp` holds 33 words.
+template <bool kTrailingBarrier = true>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* tmp, uint32_t& total) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     uint32_t x = v;
@@ -97,7 +98,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* tmp, u
     __syncthreads();
     uint32_t r = tmp[warp] + x - v;
     total = tmp[32];
-    __syncthreads();
+    // without it, the caller must pass a barrier before tmp is written again
+    if (kTrailingBarrier) __syncthreads();
     return r;
 }
 
@@ -715,7 +717,7 @@ struct RasterSmem {
     float inv255[256];
     int rowd[TS + 1], cold[TS + 1];  // candidate work of the batch, difference arrays
     uint32_t tmp[40];
-    uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics, [5] split mode
+    uint32_t misc[8];  // [0] tile ticket, [1] items staged, [2..4] statistics
     uint32_t zmaxw[kRasterWarps];  // per warp: largest stored depth of its share of the tile
 
 };
@@ -1172,8 +1174,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     if (threadIdx.x == 0) sm.misc[0] = atomicAdd(&queue[0], 1u);
     for (;;) {
     __syncthreads();
+    // misc[0] is written again only after this unit's resolve, many barriers later
     const uint32_t qi = sm.misc[0];
-    __syncthreads();
     if (qi >= nbusy * nsub) break;
     const uint32_t gt = order[qi / nsub], sub = qi % nsub;
     const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
@@ -1233,7 +1235,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             }
             if (threadIdx.x == 0) sm.misc[1] = nit;
             uint32_t itot;
-            const uint32_t iex = block_excl_scan(nitems, sm.tmp, itot);
+            // the __syncthreads_count below orders the reads of tmp before its next use
+            const uint32_t iex = block_excl_scan<false>(nitems, sm.tmp, itot);
             // entries fit while the running item count stays within the batch (a prefix)
             const bool part = (e < nent) && (nit + iex + nitems <= (uint32_t)C::IC);
             const uint32_t take = __syncthreads_count(part);
@@ -1254,13 +1257,10 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             pos += take;
             if (take < window) break;  // the batch is full
         }
-        // ---- B. divide the tile's pixels among the warps; which warps each item reaches
-        if (warp == 0) {
-            const uint32_t m = split_work<TS>(sm.rowd, sm.cold);
-            if (lane == 0) sm.misc[5] = m;
-        }
-        __syncthreads();
-        const uint32_t mode = sm.misc[5];
+        // ---- B. divide the tile's pixels among the warps (every warp computes the same
+        // choice from the batch's work histograms: no barrier to wait for one warp's);
+        // which warps each item reaches
+        const uint32_t mode = __shfl_sync(0xFFFFFFFFu, split_work<TS>(sm.rowd, sm.cold), 0);
         {
             const uint32_t t = threadIdx.x;
             uint32_t wm = 0;
