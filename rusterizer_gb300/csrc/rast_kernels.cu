@@ -1045,12 +1045,13 @@ __device__ __forceinline__ void warp_depth(RasterSmem<S, TS>& sm, uint32_t w, ui
     __syncwarp();
 }
 
-// Fragment shader and colour write of up to 32 fragments of the warp's shade ring:
+// Fragment shader and colour write of up to 32 fragments of the warp's shade ring (kept out of
+// line: the coverage loop that calls it stays small enough for the instruction cache):
 // Fragment::interpolate (src/rasterizer/mod.rs:69-100) at the point its depth-passed mask
 // selects, the draw's shader by id, then write_pixel (mod.rs:380-397) to the passed samples,
 // same-pixel fragments in rounds of increasing rank (submission order).
 template <int S, int TS>
-__device__ __forceinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head, uint32_t n,
+__device__ __noinline__ void warp_shade(RasterSmem<S, TS>& sm, uint32_t w, uint32_t head, uint32_t n,
                                            const DrawDev* __restrict__ draws, const FrameDev& f,
                                            const Scratch& s, uint32_t X0, uint32_t Y0, uint32_t& oobc) {
     using C = RasterCfg<S, TS>;
