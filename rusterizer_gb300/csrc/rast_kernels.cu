@@ -69,6 +69,15 @@ __device__ __forceinline__ uint32_t bin_entry(uint32_t tri, bool clipped, unsign
     return head | m;
 }
 
+// Programmatic dependent launch: wait until the grid launched before this one in the stream has
+// completed and its memory is visible (a no-op for a normal launch), then let the next grid's
+// CTAs be scheduled once every CTA of this one is running. First statement of every pipeline
+// kernel, so that no kernel finishes before its predecessor has.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
 
@@ -108,6 +117,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* tmp, u
 __global__ void __launch_bounds__(256) k_vertex(const DrawDev* __restrict__ draws,
                                                 const FrameDev* __restrict__ frames,
                                                 const uint2* __restrict__ vblocks, Scratch s) {
+    pdl_enter();
     __shared__ float m[16];
     const uint2 vb = vblocks[blockIdx.x];
     const DrawDev* d = &draws[vb.x];
@@ -239,6 +249,7 @@ __device__ __forceinline__ int warp_clip(ClipVert& v, int cn) {
 // counts. Grid-stride over the queue.
 __global__ void __launch_bounds__(256) k_clip(const DrawDev* __restrict__ draws,
                                               const FrameDev* __restrict__ frames, Scratch s) {
+    pdl_enter();
     const uint32_t lane = lane_id();
     const uint32_t nq = min(*(volatile unsigned int*)s.clip_n, (unsigned int)s.clip_list_cap);
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -335,6 +346,7 @@ __global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ 
                                                    const DrawDev* __restrict__ draws,
                                                    const FrameDev* __restrict__ frames,
                                                    Scratch s) {
+    pdl_enter();
     extern __shared__ uint32_t hist[];
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
@@ -367,6 +379,7 @@ __global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ 
 // One block per 32-tile group of a frame; 32 segments of chunks per tile.
 __global__ void __launch_bounds__(1024) k_scan_cols(const FrameDev* __restrict__ frames,
                                                     int nframes, Scratch s) {
+    pdl_enter();
     __shared__ uint32_t part[32][33];
     __shared__ int s_frame;
     if (threadIdx.x == 0) {
@@ -414,6 +427,7 @@ __global__ void __launch_bounds__(1024) k_scan_cols(const FrameDev* __restrict__
 // One block (1024 threads) per frame: tile_start = exclusive prefix of tile_count.
 __global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict__ frames,
                                                      Scratch s) {
+    pdl_enter();
     __shared__ uint32_t tmp[33];
     const FrameDev& f = frames[blockIdx.x];
     const uint32_t nt = f.ntiles;
@@ -460,6 +474,7 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t t) {
 __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const ChunkDev* __restrict__ chunks, const DrawDev* __restrict__ draws,
     const FrameDev* __restrict__ frames, Scratch s) {
+    pdl_enter();
     extern __shared__ uint32_t run_off[];
     __shared__ uint32_t hkey[kHashSlots];
     __shared__ uint16_t wcnt[kHashSlots][kScatterWarps];
@@ -1161,6 +1176,7 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                                                            unsigned int* __restrict__ queue,
                                                            const DrawDev* __restrict__ draws,
                                                            Scratch s) {
+    pdl_enter();
     using C = RasterCfg<S, TS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterSmem<S, TS>& sm = *reinterpret_cast<RasterSmem<S, TS>*>(smem_raw);
@@ -1488,6 +1504,7 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
 __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ frames, int nframes,
                                                    const uint32_t* __restrict__ order,
                                                    const unsigned int* __restrict__ queue, Scratch s) {
+    pdl_enter();
     constexpr int kPer = 4;
     __shared__ uint32_t tmp[2][33];
     __shared__ uint32_t base[4];
@@ -1573,6 +1590,7 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
                                                      uint32_t* __restrict__ order,
                                                      unsigned int* __restrict__ queue,
                                                      const uint32_t* __restrict__ status) {
+    pdl_enter();
     __shared__ uint32_t cnt[33], off[33];
     if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -1609,6 +1627,24 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
 
 // ===================================================================== launchers
 
+// Launch with programmatic stream serialization (see pdl_enter): the kernel may be scheduled
+// while its predecessor in the stream is still running and waits for it on entry.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                              cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <int S, int TS>
 static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
@@ -1625,26 +1661,26 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         grid_cap = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
-    k_tile_order<<<1, 1024, 0, a.stream>>>(a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
-                                           a.scratch.tile_order, a.raster_queue, a.scratch.status);
+    cudaError_t e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks,
+                               a.scratch.tile_count, a.scratch.tile_order, a.raster_queue, a.scratch.status);
+    if (e != cudaSuccess) return e;
     if (nsx > 1) {
         const unsigned sgrid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
-        k_bin_split<<<sgrid, 256, 0, a.stream>>>(a.raster_frames, a.raster_nframes,
-                                                 a.scratch.tile_order + a.raster_tile_offset, a.raster_queue,
-                                                 a.scratch);
+        e = launch_pdl(k_bin_split, sgrid, 256, 0, a.stream, a.raster_frames, a.raster_nframes,
+                       (const uint32_t*)(a.scratch.tile_order + a.raster_tile_offset),
+                       (const unsigned int*)a.raster_queue, a.scratch);
+        if (e != cudaSuccess) return e;
     }
     const unsigned long long units = (unsigned long long)a.raster_blocks * nsx * nsx;
     const unsigned grid = units < (unsigned long long)grid_cap ? (unsigned)units : (unsigned)grid_cap;
-    k_raster<S, TS><<<grid, kRasterThreads, bytes, a.stream>>>(
-        a.raster_frames, a.raster_nframes, a.scratch.tile_order + a.raster_tile_offset, a.raster_blocks,
-        nsx, a.raster_queue, a.draws, a.scratch);
-    return cudaGetLastError();
+    return launch_pdl(k_raster<S, TS>, grid, kRasterThreads, bytes, a.stream, a.raster_frames, a.raster_nframes,
+                      (const uint32_t*)(a.scratch.tile_order + a.raster_tile_offset), a.raster_blocks, nsx,
+                      a.raster_queue, a.draws, a.scratch);
 }
 
 cudaError_t launch_vertex(const LaunchArgs& a) {
     if (a.vertex_blocks == 0) return cudaSuccess;
-    k_vertex<<<a.vertex_blocks, 256, 0, a.stream>>>(a.draws, a.frames, a.vblocks, a.scratch);
-    return cudaGetLastError();
+    return launch_pdl(k_vertex, a.vertex_blocks, 256, 0, a.stream, a.draws, a.frames, a.vblocks, a.scratch);
 }
 
 cudaError_t launch_bin_count(const LaunchArgs& a) {
@@ -1656,7 +1692,9 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
         if (e != cudaSuccess) return e;
         configured = bytes;
     }
-    k_bin_count<<<a.nchunks, 256, bytes, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
+    cudaError_t e = launch_pdl(k_bin_count, a.nchunks, 256, (size_t)bytes, a.stream, a.chunks, a.draws, a.frames,
+                               a.scratch);
+    if (e != cudaSuccess) return e;
     // the straddling triangles the count queued: a grid-stride pass, one warp per triangle
     static int sms = 0;
     if (!sms) {
@@ -1668,15 +1706,16 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
     // up to four resident CTAs per SM (57 registers a thread), 32 warps per chunk: a frame of
     // a few chunks spreads its straddlers over every SM, a tiny frame launches a few CTAs
     const uint32_t grid = a.nchunks < (uint32_t)sms ? 4u * a.nchunks : (uint32_t)(4 * sms);
-    k_clip<<<grid, 256, 0, a.stream>>>(a.draws, a.frames, a.scratch);
-    return cudaGetLastError();
+    return launch_pdl(k_clip, grid, 256, 0, a.stream, a.draws, a.frames, a.scratch);
 }
 
 cudaError_t launch_scans(const LaunchArgs& a) {
-    if (a.scan_groups)
-        k_scan_cols<<<a.scan_groups, 1024, 0, a.stream>>>(a.frames, a.nframes, a.scratch);
-    if (a.nframes) k_scan_tiles<<<a.nframes, 1024, 0, a.stream>>>(a.frames, a.scratch);
-    return cudaGetLastError();
+    if (a.scan_groups) {
+        cudaError_t e = launch_pdl(k_scan_cols, a.scan_groups, 1024, 0, a.stream, a.frames, a.nframes, a.scratch);
+        if (e != cudaSuccess) return e;
+    }
+    if (a.nframes) return launch_pdl(k_scan_tiles, (unsigned)a.nframes, 1024, 0, a.stream, a.frames, a.scratch);
+    return cudaSuccess;
 }
 
 cudaError_t launch_bin_scatter(const LaunchArgs& a) {
@@ -1689,8 +1728,8 @@ cudaError_t launch_bin_scatter(const LaunchArgs& a) {
         if (e != cudaSuccess) return e;
         configured = need;
     }
-    k_bin_scatter<<<a.nchunks, kScatterThreads, need, a.stream>>>(a.chunks, a.draws, a.frames, a.scratch);
-    return cudaGetLastError();
+    return launch_pdl(k_bin_scatter, a.nchunks, kScatterThreads, (size_t)need, a.stream, a.chunks, a.draws,
+                      a.frames, a.scratch);
 }
 
 cudaError_t launch_raster(const LaunchArgs& a, int msaa, int ts) {
