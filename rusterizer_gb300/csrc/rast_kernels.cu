@@ -475,7 +475,6 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const ChunkDev* __restrict__ chunks, const DrawDev* __restrict__ draws,
     const FrameDev* __restrict__ frames, Scratch s) {
     pdl_enter();
-    extern __shared__ uint32_t run_off[];
     __shared__ uint32_t hkey[kHashSlots];
     __shared__ uint16_t wcnt[kHashSlots][kScatterWarps];
     __shared__ uint16_t slot_list[kPairsPerBatch];
@@ -491,11 +490,11 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
     const DrawDev& d = draws[ch.draw];
     const FrameDev& f = frames[d.frame];
     const uint32_t nt = f.ntiles, tx = f.tiles_x, ts = (uint32_t)f.ts;
-    const uint32_t* crow = s.counts + f.count_base + (unsigned long long)ch.row * nt;
-    // run_off[t]: the chunk's next position in tile t, loaded when the chunk first meets t
-    // (a chunk of small triangles meets few of the frame's tiles); valid: one bit per tile
-    uint32_t* valid = run_off + nt;
-    for (uint32_t t = threadIdx.x; t < (nt + 31u) / 32u; t += blockDim.x) valid[t] = 0;
+    // the chunk's row of scanned counts: its offset within each tile's list, advanced in place
+    // as the chunk's entries are placed (the row is the chunk's own and dead after this
+    // kernel); the chunk's next position in tile t is tile_start[t] + crow[t]
+    uint32_t* crow = s.counts + f.count_base + (unsigned long long)ch.row * nt;
+    const uint32_t* tstart = s.tile_start + f.tile_begin;
     for (uint32_t h = threadIdx.x; h < (uint32_t)kHashSlots; h += blockDim.x) {
         hkey[h] = kHashEmpty;
 #pragma unroll
@@ -554,13 +553,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             for (uint32_t k = threadIdx.x; k < n0; k += blockDim.x) {
                 const uint32_t ttx = x0 + k % w, tty = y0 + k / w;
                 const uint32_t t = tty * tx + ttx;
-                if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
-                    run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
-                    atomicOr(&valid[t >> 5], 1u << (t & 31u));
-                }
-                const uint32_t pos = run_off[t];
+                const uint32_t pos = tstart[t] + crow[t];
                 if (pos < cap) bins[pos] = bin_entry(fbase + base, c0, r0, ttx, tty, ts);
-                run_off[t] = pos + 1;
+                crow[t] += 1;
             }
             __syncthreads();
             base += 1;
@@ -642,17 +637,13 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
             }
         }
         __syncthreads();
-        // ---- per tile of the batch: its position before the batch (loaded from the chunk's
-        // offsets when the chunk first meets the tile), the warps' counts turned into
-        // exclusive prefixes, and the position advanced past the batch
+        // ---- per tile of the batch: its position before the batch, the warps' counts turned
+        // into exclusive prefixes, and the chunk's offset advanced past the batch
         const uint32_t ns = nslots, npairs = npairs_s;
         for (uint32_t j = threadIdx.x; j < ns; j += blockDim.x) {
             const uint32_t h = slot_list[j], t = hkey[h];
-            if (!((valid[t >> 5] >> (t & 31u)) & 1u)) {
-                run_off[t] = s.tile_start[f.tile_begin + t] + crow[t];
-                atomicOr(&valid[t >> 5], 1u << (t & 31u));
-            }
-            const uint32_t b = run_off[t];
+            const uint32_t c = crow[t];
+            const uint32_t b = tstart[t] + c;
             uint32_t tot = 0;
 #pragma unroll
             for (int w2 = 0; w2 < kScatterWarps; ++w2) {
@@ -661,7 +652,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
                 tot += c;
             }
             sbase[h] = b;
-            run_off[t] = b + tot;
+            crow[t] = c + tot;
         }
         __syncthreads();
         // ---- positions: the tile's position + earlier warps' counts + rank in the warp
@@ -1720,16 +1711,8 @@ cudaError_t launch_scans(const LaunchArgs& a) {
 
 cudaError_t launch_bin_scatter(const LaunchArgs& a) {
     if (a.nchunks == 0) return cudaSuccess;
-    static int configured = 0;
-    const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
-    const int need = bytes + (int)(((a.max_tiles + 31) / 32) * sizeof(uint32_t));
-    if (need > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
-        if (e != cudaSuccess) return e;
-        configured = need;
-    }
-    return launch_pdl(k_bin_scatter, a.nchunks, kScatterThreads, (size_t)need, a.stream, a.chunks, a.draws,
-                      a.frames, a.scratch);
+    return launch_pdl(k_bin_scatter, a.nchunks, kScatterThreads, 0, a.stream, a.chunks, a.draws, a.frames,
+                      a.scratch);
 }
 
 cudaError_t launch_raster(const LaunchArgs& a, int msaa, int ts) {
