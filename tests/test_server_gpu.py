@@ -79,3 +79,50 @@ def test_server_admission_budget():
         assert (outs[i].cpu().numpy().view(np.uint32).reshape(ref.shape) == ref).all()
     one.close()
     br.close()
+
+
+def test_bounded_waits_and_unknown_requests():
+    """A wait that runs out returns RAST_TIMEOUT and leaves the request running (a later wait
+    gets its result); poll reports NOT_READY meanwhile; an id never issued is an invalid
+    argument for poll and wait alike."""
+    torch = pytest.importorskip("torch")
+    big = scenes.soup_scene(120_000, 1024, 768, 4, np.random.default_rng(5), 256, name="big")
+    br = BatchRenderer()
+    br.add_scene(big)
+    srv = RenderServer(br, streams=1)
+    o = torch.zeros(big["height"] * big["width"], dtype=torch.int32, device="cuda")
+    rid = srv.submit(0, o.data_ptr())
+    st, _ = srv.wait(rid, timeout_ms=0)  # a whole 120k-triangle frame cannot be done already
+    assert st == _lib.TIMEOUT
+    assert srv.poll(rid)[0] in (_lib.NOT_READY, _lib.OK, _lib.TEXTURE_OOB)
+    st, lat = srv.wait(rid, timeout_ms=60000)
+    assert st in (_lib.OK, _lib.TEXTURE_OOB) and lat > 0.0
+    assert srv.poll(rid)[0] == st
+    assert srv.poll(rid + 1000)[0] == _lib.INVALID_ARG
+    assert srv.wait(rid + 1000, timeout_ms=10)[0] == _lib.INVALID_ARG
+    ref = np.zeros((big["height"], big["width"]), np.uint32)
+    br.render([ref], indices=[0])
+    assert (o.cpu().numpy().view(np.uint32).reshape(ref.shape) == ref).all()
+    srv.close()
+    br.close()
+
+
+def test_destroy_drains_requests_never_waited_for():
+    """Requests whose submitter never waits (a dropped client) are still rendered and the
+    server shuts down cleanly: destroy drains the queue."""
+    torch = pytest.importorskip("torch")
+    sc = pool()
+    br = BatchRenderer()
+    for s in sc:
+        br.add_scene(s)
+    srv = RenderServer(br, streams=2)
+    outs = [torch.zeros(s["height"] * s["width"], dtype=torch.int32, device="cuda") for s in sc]
+    for i in range(len(sc)):
+        srv.submit(i, outs[i].data_ptr())
+    srv.close()  # no wait on any request
+    torch.cuda.synchronize()
+    for i, s in enumerate(sc):
+        ref = np.zeros((s["height"], s["width"]), np.uint32)
+        br.render([ref], indices=[i])
+        assert (outs[i].cpu().numpy().view(np.uint32).reshape(ref.shape) == ref).all(), s["name"]
+    br.close()
