@@ -192,8 +192,8 @@ __device__ __forceinline__ float edge_eval(float nx, float ny, float px, float p
 }
 
 // edge_eval without the leading 0.0 + : the same value except that an exact zero can come out
-// as -0.0 instead of +0.0, which no edge test (e > 0, e < 0, tie rule) can tell apart. Used
-// where the value only feeds the edge test.
+// as -0.0 instead of +0.0, which no edge test (e > 0, e < 0, tie rule) can tell apart, nor the
+// sample depth computed from it (interp_depth_fast). The coverage loop's form.
 __device__ __forceinline__ float edge_eval_test(float nx, float ny, float px, float py, float x, float y) {
     const float dx = x - px, dy = y - py;
     return nx * dx + ny * dy;
@@ -216,8 +216,9 @@ __device__ __forceinline__ float clamp01_nan(float x) {
 
 // RasterizerTriangle::fragment's interpolate_depth (src/rasterizer/mod.rs:226-236):
 // b0 = clamp(e1 inv), b1 = clamp(e2 inv), b2 = clamp((1 - b0) - b1), z = (b0 z0 + b1 z1) +
-// b2 z2 with inv = 1 / triangle_2x_area, here over edge values that may carry either sign of zero (edge_eval_test) and with
-// clamp01_nan. The depth comes out bit for bit as the reference's (edge values with the
+// b2 z2 with inv = 1 / triangle_2x_area, here over edge values that may carry either sign of
+// zero (edge_eval_test) and with clamp01_nan. The depth comes out bit for bit as the
+// reference's (edge values with the
 // leading 0 +, clamp01), except for the payload of a NaN (a NaN depth never passes the depth
 // test, and a shader that reads it saturates it to 0): flipping the sign of a zero b0 or b1
 // flips only the sign of a zero product b * z, and the sum can then only change from +0 to
