@@ -77,11 +77,14 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def committed_traffic(cfg):
+def committed_profile(cfg, key=None):
+    """From the committed ncu capture of the raster kernel (profiles/traffic.json): DRAM bytes
+    per launch, or with key="issue_active" the fraction of cycles the schedulers issued."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get(str(cfg))
+            d = json.load(f)
+        return (d.get(key) or {}).get(str(cfg)) if key else d.get(str(cfg))
     except Exception:
         return None
 
@@ -404,7 +407,9 @@ def run_ours(args):
             "wall_ms_per_step": 1000 * wall / args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": committed_traffic(args.config),
+                         "traffic": committed_profile(args.config),
+                         # the bound that holds: instruction issue, from the same ncu capture
+                         "issue_active_ncu": committed_profile(args.config, "issue_active"),
                          "algorithmic_bytes_per_frame": bytes_frame,
                          "dominant_stage": names[dom]},
             "cpu_baseline": cpu,
