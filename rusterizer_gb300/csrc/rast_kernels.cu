@@ -13,7 +13,9 @@
 // No kernel waits on another CTA; every loop is bounded by sizes read from descriptors.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 
 #include "rast_device.cuh"
 #include "rast_kernels.h"
@@ -1636,20 +1638,35 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned 
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// Multiprocessor count of the current device, queried once (host threads may launch at once).
+static int sm_count() {
+    static std::atomic<int> sms{0};
+    int n = sms.load(std::memory_order_relaxed);
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+        sms.store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
 template <int S, int TS>
 static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
-    static int grid_cap = 0;
+    // persistent grid: resident CTAs per SM x SMs, set up once (every thread computes the same)
+    static std::atomic<int> grid_cap_once{0};
+    int grid_cap = grid_cap_once.load(std::memory_order_acquire);
     if (!grid_cap) {
         cudaError_t e = cudaFuncSetAttribute(k_raster<S, TS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int per = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<S, TS>, kRasterThreads, bytes);
         if (e != cudaSuccess) return e;
-        grid_cap = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+        grid_cap = (per > 0 ? per : 1) * sm_count();
+        grid_cap_once.store(grid_cap, std::memory_order_release);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
     cudaError_t e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks,
@@ -1676,24 +1693,24 @@ cudaError_t launch_vertex(const LaunchArgs& a) {
 
 cudaError_t launch_bin_count(const LaunchArgs& a) {
     if (a.nchunks == 0) return cudaSuccess;
+    // the kernel's dynamic shared-memory limit only ever grows, under a lock: a smaller value
+    // set by another host thread must not undercut a concurrent larger launch
+    static std::mutex mu;
     static int configured = 0;
     const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
-    if (bytes > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        configured = bytes;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (bytes > configured) {
+            cudaError_t e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e != cudaSuccess) return e;
+            configured = bytes;
+        }
     }
     cudaError_t e = launch_pdl(k_bin_count, a.nchunks, 256, (size_t)bytes, a.stream, a.chunks, a.draws, a.frames,
                                a.scratch);
     if (e != cudaSuccess) return e;
     // the straddling triangles the count queued: a grid-stride pass, one warp per triangle
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    const int sms = sm_count();
     // up to four resident CTAs per SM (57 registers a thread), 32 warps per chunk: a frame of
     // a few chunks spreads its straddlers over every SM, a tiny frame launches a few CTAs
     const uint32_t grid = a.nchunks < (uint32_t)sms ? 4u * a.nchunks : (uint32_t)(4 * sms);
