@@ -109,11 +109,14 @@ rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out_device);
  * output, plus host row-major world/view/proj matrices. All intermediate buffers live in one
  * 32 MiB array in device memory owned by the library and held on every GPU that loads it
  * until exit; frames that need more, or more than 262144 vertices or triangles, return
- * RAST_INVALID_ARG without launching anything. The first call on a device looks up that
- * array's address (make it before any stream capture). Work runs on `stream`
- * (cudaStream_t, NULL = legacy default) and the call waits for it to finish. Calls share the
- * array: calls whose GPU work overlaps race and must be serialised by the caller. Same image,
- * status and bit-exactness as rast_framebuffer for the same inputs. */
+ * RAST_INVALID_ARG without launching anything. A frame whose bins or clipped polygons
+ * overflow the first estimate is run again with the measured sizes (up to three runs, as
+ * rast_framebuffer does) while they still fit the array, else RAST_INVALID_ARG. The first
+ * call on a device looks up that array's address (make it before any stream capture). Work
+ * runs on `stream` (cudaStream_t, NULL = legacy default) and the call waits for it to finish.
+ * Calls share the array: calls whose GPU work overlaps race and must be serialised by the
+ * caller. Host stack use is small (the descriptor staging is static, under a lock). Same
+ * image, status and bit-exactness as rast_framebuffer for the same inputs. */
 rast_status rast_render_noalloc(int width, int height, int msaa, int tile, float clear_depth,
                                 const float* d_pos, const float* d_uv, const float* d_rgba,
                                 uint32_t nverts, const uint32_t* d_idx, uint32_t ntris,
@@ -175,14 +178,21 @@ rast_status rast_server_create(rast_ctx* ctx, const rast_server_config* cfg, ras
  * scene alone exceeds the budget. Thread-safe. */
 rast_status rast_server_submit(rast_server* srv, const rast_scene* scene, uint64_t* request_id);
 /* RAST_NOT_READY until the request has finished; then its status, and latency from submit to
- * completion in ms. */
+ * completion in ms. Returning the final status releases the request's record: a later poll or
+ * wait on the same id is RAST_INVALID_ARG. Finished requests nobody collects are kept for the
+ * most recent 65536 completions only, so a server that runs indefinitely stays bounded. */
 rast_status rast_server_poll(rast_server* srv, uint64_t request_id, double* latency_ms);
-/* Waits up to timeout_ms (negative = no limit) for the request; RAST_TIMEOUT when it expires. */
+/* Waits up to timeout_ms (negative = no limit) for the request; RAST_TIMEOUT when it expires
+ * (the request keeps running). Returning the final status releases the record, as for poll. */
 rast_status rast_server_wait(rast_server* srv, uint64_t request_id, int timeout_ms, double* latency_ms);
-/* Latency percentiles and throughput over the requests completed since the last reset. */
+/* Latency percentiles over the most recent 2^20 requests completed since the last reset;
+ * completed and requests_per_s count every completion since the reset. */
 rast_status rast_server_stats(rast_server* srv, double* p50_ms, double* p99_ms, uint64_t* completed,
                               double* requests_per_s, double* mean_batch);
 rast_status rast_server_reset_stats(rast_server* srv);
+/* Requests queued, rendering now, and request records held (queued, running, finished and not
+ * yet collected). */
+rast_status rast_server_info(rast_server* srv, uint64_t* queued, uint64_t* running, uint64_t* tracked);
 /* Drains the queue and stops the dispatcher. */
 rast_status rast_server_destroy(rast_server* srv);
 

@@ -56,6 +56,7 @@ SIGNATURES = {
     "rast_server_stats": (_i, [_vp, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double), _u64p,
                                _c.POINTER(_c.c_double), _c.POINTER(_c.c_double)]),
     "rast_server_reset_stats": (_i, [_vp]),
+    "rast_server_info": (_i, [_vp, _u64p, _u64p, _u64p]),
     "rast_server_destroy": (_i, [_vp]),
     "rast_stats": (_i, [_vp, _u64p, _u64p, _u64p]),
     "rast_stream": (_vp, [_vp]),

@@ -1638,16 +1638,30 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned 
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
-// Multiprocessor count of the current device, queried once (host threads may launch at once).
+// Per-device launch set-up (multiprocessor count, raised shared-memory limits, persistent grid
+// sizes), looked up once per device: a process may render on several GPUs, and
+// cudaFuncSetAttribute applies to the current device only. Host threads may launch at once.
+constexpr int kMaxDevices = 64;
+
+static int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return -1;
+    }
+    return dev;
+}
+
+// Multiprocessor count of the current device.
 static int sm_count() {
-    static std::atomic<int> sms{0};
-    int n = sms.load(std::memory_order_relaxed);
+    static std::atomic<int> sms[kMaxDevices];
+    const int dev = current_device();
+    if (dev < 0) return 1;
+    int n = sms[dev].load(std::memory_order_relaxed);
     if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (n <= 0) n = 1;
-        sms.store(n, std::memory_order_relaxed);
+        sms[dev].store(n, std::memory_order_relaxed);
     }
     return n;
 }
@@ -1655,9 +1669,12 @@ static int sm_count() {
 template <int S, int TS>
 static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
-    // persistent grid: resident CTAs per SM x SMs, set up once (every thread computes the same)
-    static std::atomic<int> grid_cap_once{0};
-    int grid_cap = grid_cap_once.load(std::memory_order_acquire);
+    // persistent grid: resident CTAs per SM x SMs, set up once per device (every thread
+    // computes the same)
+    static std::atomic<int> grid_cap_once[kMaxDevices];
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    int grid_cap = grid_cap_once[dev].load(std::memory_order_acquire);
     if (!grid_cap) {
         cudaError_t e = cudaFuncSetAttribute(k_raster<S, TS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -1666,7 +1683,7 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<S, TS>, kRasterThreads, bytes);
         if (e != cudaSuccess) return e;
         grid_cap = (per > 0 ? per : 1) * sm_count();
-        grid_cap_once.store(grid_cap, std::memory_order_release);
+        grid_cap_once[dev].store(grid_cap, std::memory_order_release);
     }
     if (a.raster_blocks == 0) return cudaSuccess;
     cudaError_t e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks,
@@ -1693,17 +1710,19 @@ cudaError_t launch_vertex(const LaunchArgs& a) {
 
 cudaError_t launch_bin_count(const LaunchArgs& a) {
     if (a.nchunks == 0) return cudaSuccess;
-    // the kernel's dynamic shared-memory limit only ever grows, under a lock: a smaller value
-    // set by another host thread must not undercut a concurrent larger launch
+    // the kernel's dynamic shared-memory limit (per device) only ever grows, under a lock: a
+    // smaller value set by another host thread must not undercut a concurrent larger launch
     static std::mutex mu;
-    static int configured = 0;
+    static int configured[kMaxDevices] = {};
     const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
     {
         std::lock_guard<std::mutex> lk(mu);
-        if (bytes > configured) {
+        if (bytes > configured[dev]) {
             cudaError_t e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
             if (e != cudaSuccess) return e;
-            configured = bytes;
+            configured[dev] = bytes;
         }
     }
     cudaError_t e = launch_pdl(k_bin_count, a.nchunks, 256, (size_t)bytes, a.stream, a.chunks, a.draws, a.frames,

@@ -3,10 +3,16 @@
 // Submitters enqueue scenes; one dispatcher thread owns up to two launch slots, each with its
 // own engine (scratch buffers, descriptor staging, CUDA stream). Whenever a slot is free, the
 // dispatcher takes queued requests in arrival order while they fit the HBM budget, renders
-// them as one batch on that slot's stream and records an event; completion is detected by
-// polling the event, so a second batch can be launched (on the other slot) while the first
-// still runs and the two overlap on the device. A batch that overflowed its bin or clip
-// capacity is re-queued at the front with the measured sizes remembered per scene shape.
+// them as one batch on that slot's stream and enqueues a host callback behind it; the
+// callback marks the slot complete and wakes the dispatcher (no polling), so a second batch
+// can be launched (on the other slot) while the first still runs and the two overlap on the
+// device. A batch that overflowed its bin or clip capacity is re-queued at the front with the
+// measured sizes remembered per scene shape.
+//
+// Memory stays bounded however long the server runs: a request's record is released when a
+// wait or poll has returned its final status; finished records nobody collects are kept for
+// the most recent kMaxUnclaimed requests only; latency statistics cover the most recent
+// kMaxLatencySamples completions.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,14 +44,18 @@ struct Request {
     bool done = false;
 };
 
+constexpr size_t kMaxUnclaimed = size_t(1) << 16;        // finished records kept uncollected
+constexpr size_t kMaxLatencySamples = size_t(1) << 20;  // latency window of the statistics
+
 struct Slot {
     Engine E;
     bool busy = false;
+    bool complete = false;  // set by the host callback behind the slot's batch
     std::vector<uint64_t> ids;
     std::vector<FrameJob> jobs;
     uint64_t bytes = 0;
-    cudaEvent_t done = nullptr;
     HostBuf<unsigned long long> need;
+    void* server = nullptr;
 };
 
 using ShapeKey = std::tuple<uint32_t, int, int, int, int>;  // mesh, width, height, msaa, tile
@@ -79,10 +89,45 @@ struct rast_server {
     int nslots = 1;
     uint64_t inflight = 0;
     std::map<ShapeKey, uint64_t> bins_hint;
-    // statistics since the last reset
+    std::deque<uint64_t> unclaimed;  // finished requests in completion order (maybe collected)
+    // statistics since the last reset: a ring of the most recent latencies
     std::vector<double> lat_ms;
+    size_t lat_next = 0;
+    uint64_t completed = 0;
     Clock::time_point t_first{}, t_last{};
     uint64_t batches = 0, batch_scenes = 0;
+
+    void record_latency(double ms) {
+        if (lat_ms.size() < kMaxLatencySamples) {
+            lat_ms.push_back(ms);
+        } else {
+            lat_ms[lat_next] = ms;
+            lat_next = (lat_next + 1) % kMaxLatencySamples;
+        }
+        ++completed;
+    }
+
+    // A request finished: keep its record for the submitter, dropping the oldest uncollected
+    // records beyond kMaxUnclaimed (ids already collected are skipped).
+    void retire(uint64_t id) {
+        unclaimed.push_back(id);
+        while (unclaimed.size() > kMaxUnclaimed) {
+            reqs.erase(unclaimed.front());
+            unclaimed.pop_front();
+        }
+    }
+
+    // Host callback behind a slot's batch (runs on a CUDA driver thread once the batch and its
+    // status copies are complete; it makes no CUDA call).
+    static void CUDART_CB on_slot_done(void* p) {
+        Slot* sl = static_cast<Slot*>(p);
+        rast_server* srv = static_cast<rast_server*>(sl->server);
+        {
+            std::lock_guard<std::mutex> lk(srv->mu);
+            sl->complete = true;
+        }
+        srv->cv_work.notify_one();
+    }
 
     int tile_of(const rast_scene& s) const {
         int req = s.tile ? s.tile : ctx->tuned_tile[s.msaa == 4 ? 1 : 0];
@@ -146,7 +191,7 @@ struct rast_server {
             cudaMemcpyAsync(sl.E.h_state, sl.E.d_state, sizeof(DeviceState), cudaMemcpyDeviceToHost, sl.E.stream);
             cudaMemcpyAsync(sl.need.p, sl.E.frame_need.p, nf * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, sl.E.stream);
-            ok = cudaEventRecord(sl.done, sl.E.stream) == cudaSuccess;
+            ok = cudaLaunchHostFunc(sl.E.stream, on_slot_done, &sl) == cudaSuccess;
         }
         lk.lock();
         if (!ok) {
@@ -157,6 +202,7 @@ struct rast_server {
                 r.status = st != RAST_OK ? st : RAST_CUDA_ERROR;
                 r.done = true;
                 r.t_done = now;
+                retire(id);
             }
             inflight -= sl.bytes;
             sl.busy = false;
@@ -165,9 +211,10 @@ struct rast_server {
         return true;
     }
 
-    // Called with the lock held for a slot whose event completed.
+    // Called with the lock held for a slot whose host callback ran: the batch and its status
+    // copies are complete (no CUDA call here: the callback of the other slot takes this lock).
     void finish(Slot& sl) {
-        cudaStreamSynchronize(sl.E.stream);
+        sl.complete = false;
         const uint32_t status = sl.E.h_state->status;
         const Clock::time_point now = Clock::now();
         const bool overflow = (status & (ST_BIN_OVERFLOW | ST_CLIP_STORE_OVERFLOW)) != 0;
@@ -196,9 +243,10 @@ struct rast_server {
             r.status = rs;
             r.done = true;
             r.t_done = now;
-            lat_ms.push_back(std::chrono::duration<double, std::milli>(now - r.t_submit).count());
+            record_latency(std::chrono::duration<double, std::milli>(now - r.t_submit).count());
             if (t_first == Clock::time_point{}) t_first = r.t_submit;
             t_last = now;
+            retire(id);
         }
         ++batches;
         batch_scenes += sl.ids.size();
@@ -210,17 +258,17 @@ struct rast_server {
         for (;;) {
             bool progress = false;
             for (int i = 0; i < nslots; ++i)
-                if (slots[i].busy && cudaEventQuery(slots[i].done) == cudaSuccess) {
+                if (slots[i].busy && slots[i].complete) {
                     finish(slots[i]);
                     progress = true;
                 }
-            cudaGetLastError();
             for (int i = 0; i < nslots; ++i)
                 if (!slots[i].busy && launch_one(slots[i], lk)) progress = true;
             bool any_busy = false;
             for (int i = 0; i < nslots; ++i) any_busy |= slots[i].busy;
             if (stop && queue.empty() && !any_busy) break;
-            if (!progress) cv_work.wait_for(lk, std::chrono::microseconds(any_busy ? 20 : 500));
+            // woken by a submit, a slot's callback or destroy; the timeout is only a backstop
+            if (!progress) cv_work.wait_for(lk, std::chrono::milliseconds(50));
         }
     }
 };
@@ -236,8 +284,8 @@ rast_status rast_server_create(rast_ctx* c, const rast_server_config* cfg, rast_
     if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = 40ull << 30;
     s->nslots = (s->cfg.streams == 2 && !s->cfg.one_per_launch) ? 2 : 1;
     for (int i = 0; i < s->nslots; ++i) {
-        if (!s->slots[i].E.init() ||
-            cudaEventCreateWithFlags(&s->slots[i].done, cudaEventDisableTiming) != cudaSuccess) {
+        s->slots[i].server = s;
+        if (!s->slots[i].E.init()) {
             delete s;
             return RAST_CUDA_ERROR;
         }
@@ -282,7 +330,9 @@ rast_status rast_server_poll(rast_server* s, uint64_t id, double* latency_ms) {
     if (!it->second.done) return RAST_NOT_READY;
     if (latency_ms)
         *latency_ms = std::chrono::duration<double, std::milli>(it->second.t_done - it->second.t_submit).count();
-    return it->second.status;
+    const rast_status st = it->second.status;
+    s->reqs.erase(it);  // the final status has been collected
+    return st;
 }
 
 rast_status rast_server_wait(rast_server* s, uint64_t id, int timeout_ms, double* latency_ms) {
@@ -301,7 +351,9 @@ rast_status rast_server_wait(rast_server* s, uint64_t id, int timeout_ms, double
     if (it == s->reqs.end()) return RAST_INVALID_ARG;
     if (latency_ms)
         *latency_ms = std::chrono::duration<double, std::milli>(it->second.t_done - it->second.t_submit).count();
-    return it->second.status;
+    const rast_status st = it->second.status;
+    s->reqs.erase(it);  // the final status has been collected
+    return st;
 }
 
 rast_status rast_server_stats(rast_server* s, double* p50, double* p99, uint64_t* completed,
@@ -317,10 +369,10 @@ rast_status rast_server_stats(rast_server* s, double* p50, double* p99, uint64_t
     };
     if (p50) *p50 = pct(0.50);
     if (p99) *p99 = pct(0.99);
-    if (completed) *completed = v.size();
+    if (completed) *completed = s->completed;
     if (rps) {
         const double span = std::chrono::duration<double>(s->t_last - s->t_first).count();
-        *rps = span > 0 ? (double)v.size() / span : 0.0;
+        *rps = span > 0 ? (double)s->completed / span : 0.0;
     }
     if (mean_batch) *mean_batch = s->batches ? (double)s->batch_scenes / (double)s->batches : 0.0;
     return RAST_OK;
@@ -330,11 +382,23 @@ rast_status rast_server_reset_stats(rast_server* s) {
     if (!s) return RAST_INVALID_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat_ms.clear();
+    s->lat_next = 0;
+    s->completed = 0;
     s->t_first = Clock::time_point{};
     s->t_last = Clock::time_point{};
     s->batches = s->batch_scenes = 0;
-    for (auto it = s->reqs.begin(); it != s->reqs.end();)
-        it = it->second.done ? s->reqs.erase(it) : std::next(it);
+    return RAST_OK;
+}
+
+rast_status rast_server_info(rast_server* s, uint64_t* queued, uint64_t* running, uint64_t* tracked) {
+    if (!s) return RAST_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint64_t run = 0;
+    for (int i = 0; i < s->nslots; ++i)
+        if (s->slots[i].busy) run += s->slots[i].ids.size();
+    if (queued) *queued = s->queue.size();
+    if (running) *running = run;
+    if (tracked) *tracked = s->reqs.size();
     return RAST_OK;
 }
 
@@ -346,8 +410,6 @@ rast_status rast_server_destroy(rast_server* s) {
     }
     s->cv_work.notify_all();
     if (s->th.joinable()) s->th.join();
-    for (int i = 0; i < s->nslots; ++i)
-        if (s->slots[i].done) cudaEventDestroy(s->slots[i].done);
     delete s;
     return RAST_OK;
 }

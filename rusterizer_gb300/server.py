@@ -49,6 +49,12 @@ class RenderServer:
         return {"p50_ms": p50.value, "p99_ms": p99.value, "completed": n.value, "req_per_s": rps.value,
                 "mean_batch": mb.value}
 
+    def info(self):
+        """Requests queued, rendering now, and request records the server holds."""
+        q, r, t = (ctypes.c_uint64() for _ in range(3))
+        check(_lib.load().rast_server_info(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(t)))
+        return {"queued": q.value, "running": r.value, "tracked": t.value}
+
     def reset_stats(self):
         check(_lib.load().rast_server_reset_stats(self._h))
 

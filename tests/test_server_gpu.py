@@ -83,8 +83,8 @@ def test_server_admission_budget():
 
 def test_bounded_waits_and_unknown_requests():
     """A wait that runs out returns RAST_TIMEOUT and leaves the request running (a later wait
-    gets its result); poll reports NOT_READY meanwhile; an id never issued is an invalid
-    argument for poll and wait alike."""
+    gets its result and releases the record); poll reports NOT_READY meanwhile; an id never
+    issued is an invalid argument for poll and wait alike."""
     torch = pytest.importorskip("torch")
     big = scenes.soup_scene(120_000, 1024, 768, 4, np.random.default_rng(5), 256, name="big")
     br = BatchRenderer()
@@ -97,7 +97,9 @@ def test_bounded_waits_and_unknown_requests():
     assert srv.poll(rid)[0] in (_lib.NOT_READY, _lib.OK, _lib.TEXTURE_OOB)
     st, lat = srv.wait(rid, timeout_ms=60000)
     assert st in (_lib.OK, _lib.TEXTURE_OOB) and lat > 0.0
-    assert srv.poll(rid)[0] == st
+    # the final status has been collected: the record is released
+    assert srv.poll(rid)[0] == _lib.INVALID_ARG
+    assert srv.info()["tracked"] == 0
     assert srv.poll(rid + 1000)[0] == _lib.INVALID_ARG
     assert srv.wait(rid + 1000, timeout_ms=10)[0] == _lib.INVALID_ARG
     ref = np.zeros((big["height"], big["width"]), np.uint32)
@@ -125,4 +127,44 @@ def test_destroy_drains_requests_never_waited_for():
         ref = np.zeros((s["height"], s["width"]), np.uint32)
         br.render([ref], indices=[i])
         assert (outs[i].cpu().numpy().view(np.uint32).reshape(ref.shape) == ref).all(), s["name"]
+    br.close()
+
+
+def test_request_table_stays_bounded():
+    """120 000 small requests: collected ones leave the table at once, and of requests nobody
+    waits for only the most recent 65 536 finished records are kept, so a server that runs
+    indefinitely holds bounded memory; the latency statistics still count every completion."""
+    torch = pytest.importorskip("torch")
+    tiny = scenes.soup_scene(40, 32, 32, 4, np.random.default_rng(8), 16, name="tiny")
+    br = BatchRenderer()
+    br.add_scene(tiny)
+    ref = np.zeros((32, 32), np.uint32)
+    br.render([ref], indices=[0])
+    srv = RenderServer(br, streams=2)
+    o = torch.zeros(32 * 32, dtype=torch.int32, device="cuda")
+    n, peak = 50_000, 0
+    for k in range(0, n, 1000):
+        rids = [srv.submit(0, o.data_ptr()) for _ in range(1000)]
+        for rid in rids:
+            assert srv.wait(rid, timeout_ms=60000)[0] in (_lib.OK, _lib.TEXTURE_OOB)
+        peak = max(peak, srv.info()["tracked"])
+    assert srv.info()["tracked"] == 0 and peak <= 1000
+    # 70 000 more that nobody collects
+    n2 = 70_000
+    for _ in range(n2):
+        srv.submit(0, o.data_ptr())
+    deadline = 600
+    import time
+    t0 = time.time()
+    while True:
+        info = srv.info()
+        if info["queued"] == 0 and info["running"] == 0:
+            break
+        assert time.time() - t0 < deadline
+        time.sleep(0.01)
+    assert srv.info()["tracked"] == 65536
+    assert srv.stats()["completed"] == n + n2
+    torch.cuda.synchronize()
+    assert (o.cpu().numpy().view(np.uint32).reshape(32, 32) == ref).all()
+    srv.close()
     br.close()

@@ -86,3 +86,54 @@ def test_noalloc_out_of_range_index_reported():
     assert _noalloc(torch, bad, out) == _lib.INVALID_ARG
     assert _noalloc(torch, scene, out) == _lib.OK
     assert (out.cpu().numpy().view(np.uint32).reshape(H, W) == ref).all()
+
+
+def _ndc_scene(width, height, pos, idx, name):
+    """A one-draw scene given directly in clip space (identity world, view and projection),
+    textured with a 64x64 checkerboard."""
+    pos = np.asarray(pos, np.float32)
+    n = len(pos)
+    rng = np.random.default_rng(5)
+    eye = np.eye(4, dtype=np.float32)
+    return {"name": name, "width": width, "height": height, "msaa": 4,
+            "clear_depth": float(np.finfo(np.float32).max), "view": eye, "proj": eye,
+            "textures": [scenes.checkerboard(64, 8)],
+            "draws": [{"pos": pos, "uv": rng.random((n, 2), dtype=np.float32),
+                       "rgba": rng.random((n, 4), dtype=np.float32),
+                       "idx": np.asarray(idx, np.uint32).reshape(-1, 3), "world": eye, "fs": 0}]}
+
+
+def many_small_triangles(ntris=190_000):
+    """ntris triangles over 12 vertices on a 64x64 target: four small clockwise triangles,
+    each inside one 16-pixel bin, repeated (the binning then needs 743 chunks of 256
+    triangles and about 30 MiB of scratch)."""
+    pos, tris = [], []
+    for k, (cx, cy) in enumerate([(-0.6, 0.6), (0.5, 0.55), (-0.45, -0.5), (0.6, -0.6)]):
+        z = 0.1 * k
+        pos += [(cx - 0.08, cy - 0.06, z), (cx, cy + 0.09, z), (cx + 0.07, cy - 0.05, z)]
+        tris.append((3 * k, 3 * k + 1, 3 * k + 2))
+    idx = np.array([tris[i % 4] for i in range(ntris)], np.uint32)
+    return _ndc_scene(64, 64, pos, idx, "many_small")
+
+
+def screen_quad_4k():
+    """Two triangles covering a 3840x2160 target: every bin holds both, more entries than the
+    first bin estimate (4 per triangle + 1 per bin + 1024), so the frame runs twice."""
+    pos = [(-1.5, -1.5, 0.2), (-1.5, 1.5, 0.2), (1.5, 1.5, 0.2), (1.5, -1.5, 0.2)]
+    return _ndc_scene(3840, 2160, pos, [(0, 1, 2), (0, 2, 3)], "quad_4k")
+
+
+@pytest.mark.parametrize("make,tile", [(many_small_triangles, 16), (screen_quad_4k, 0)])
+def test_noalloc_large_chunk_counts_and_bin_regrowth(make, tile):
+    torch = pytest.importorskip("torch")
+    scene = make()
+    ref, st, r = renderer.render_scene(scene, tile=tile)
+    r.close()
+    assert st == _lib.OK
+    assert (ref != 0xFF191919).any(), "the scene covers pixels"
+    H, W = scene["height"], scene["width"]
+    out = torch.zeros(H * W, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        out.fill_(0)
+        assert _noalloc(torch, scene, out, tile=tile) == _lib.OK
+        assert (out.cpu().numpy().view(np.uint32).reshape(H, W) == ref).all()
