@@ -123,15 +123,65 @@ REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_c
            0x100: "display_clock_setting"}
 
 
+class _Nvml:
+    """The few NVML reads the clock sampler needs, through ctypes (read-only queries)."""
+
+    def __init__(self, pci_bus_id, index):
+        import ctypes
+        self.L = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.L.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        ok = pci_bus_id is not None and self.L.nvmlDeviceGetHandleByPciBusId_v2(
+            pci_bus_id.encode(), ctypes.byref(self.h)) == 0
+        if not ok and self.L.nvmlDeviceGetHandleByIndex_v2(int(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.ct = ctypes
+        self._reasons = getattr(self.L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.L.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def read(self):
+        c = self.ct
+        sm, mx, rs = c.c_uint(), c.c_uint(), c.c_ulonglong()
+        if self.L.nvmlDeviceGetClockInfo(self.h, 1, c.byref(sm)) != 0:
+            return None
+        self.L.nvmlDeviceGetMaxClockInfo(self.h, 1, c.byref(mx))
+        self._reasons(self.h, c.byref(rs))
+        return sm.value, mx.value, rs.value
+
+    def close(self):
+        self.L.nvmlShutdown()
+
+
+def _pci_bus_id(index):
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(index)
+        return "%08X:%02X:%02X.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+    except Exception:
+        return None
+
+
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled every 2 ms through NVML while it is
+    open (the GPU is found by its PCI bus id); nvidia-smi at 200 ms where NVML is unavailable."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self.samples = []
+        self.nvml = None
+        self.stop = threading.Event()
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(_pci_bus_id(self.index), self.index)
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
@@ -143,11 +193,22 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.is_set():
+            r = self.nvml.read()
+            if r:
+                self.samples.append(r)
+            self.stop.wait(0.002)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=2)
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -158,23 +219,26 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], None, set()
+        rows = list(self.samples)
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 3:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
-                bits = int(parts[2], 16) if parts[2].startswith("0x") else int(parts[2])
+                rows.append((float(parts[0]), float(parts[1]),
+                             int(parts[2], 16) if parts[2].startswith("0x") else int(parts[2])))
             except ValueError:
                 continue
-            for b, n in REASONS.items():
-                if bits & b and n != "gpu_idle":
+        for a, b, bits in rows:
+            sm.append(float(a))
+            mx = float(b)
+            for bit, n in REASONS.items():
+                if bits & bit and n != "gpu_idle":
                     reasons.add(n)
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvml 2 ms" if self.samples else "nvidia-smi 200 ms"}
 
 
 def cpu_baseline(scene, seconds, nthreads):
