@@ -61,6 +61,13 @@ rast_status rast_set_clear_depth(rast_ctx* ctx, float depth);
  * triangles or more, else 16 (either one when the other would exceed 16384 tiles). */
 rast_status rast_set_tile_size(rast_ctx* ctx, int tile);
 
+/* How raster tiles are split between the two raster kernels (no counterpart in the reference,
+ * whose pixel loop is serial): bins with at least min_entries entries (rounded down to a power
+ * of two) are rastered by a whole CTA per tile, the others by one warp per tile. 0 sends every
+ * bin to the CTA-wide kernel (the default), 0xFFFFFFFF every bin to the warp kernel. Results
+ * are identical either way; only speed changes. */
+rast_status rast_set_heavy_tile_entries(rast_ctx* ctx, uint32_t min_entries);
+
 /* Upload a mesh (Mesh{vertices, indices, attributes}, src/mesh.rs:5-12) so that it stays
  * resident. pos: nverts*3 f32; uv: nverts*2 f32; rgba: nverts*4 f32 or NULL (colour
  * (0,0,0,0)); idx: ntris*3 u32, each < nverts (primitive_assembly would panic otherwise,

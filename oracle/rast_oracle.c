@@ -11,11 +11,14 @@
  * a texel read past the end of the texture buffer (ORACLE_TEXTURE_OOB; the read then uses
  * texel 0) and an index >= nverts (ORACLE_INVALID_ARG; the draw is refused).
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers under -std=c11 */
 #include "rast_oracle.h"
 
 #include <float.h>
 #include <math.h>
 #include <pthread.h>
+#include <sched.h>
+#include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -449,7 +452,9 @@ void oracle_tiles_get(const oracle_tiles* t, int i, uint64_t out[4]) {
  * is ignored) */
 void oracle_tiles_mark(oracle_tiles* t, uint64_t row, uint64_t col) {
     uint64_t idx = (row / TILE_SIZE) * t->n_horizontal + (col / TILE_SIZE);
-    if (idx < (uint64_t)t->n) t->mask[t->mask_idx][idx] = 1;
+    /* written once per tile and frame: band threads that share a cache line of the mask then
+     * only read it */
+    if (idx < (uint64_t)t->n && !t->mask[t->mask_idx][idx]) t->mask[t->mask_idx][idx] = 1;
 }
 /* BufferTiles::next, buffers.rs:58-63 */
 void oracle_tiles_next(oracle_tiles* t) {
@@ -484,7 +489,44 @@ struct oracle_ctx {
     uint64_t tri_base; /* running triangle index over draws, for the fragment log */
     uint32_t* log;
     uint64_t log_cap, log_n;
+    int nthreads; /* threads of the last draw, reused by the resolve */
 };
+
+/* ------------------------------------------------------------------ threads */
+
+/* Runs fn(arg, part, nparts) for part = 0 .. nparts-1 on nparts threads (the caller's thread
+ * runs part 0). The reference is single-threaded; this only spreads independent work. */
+typedef void (*part_fn)(void* arg, int part, int nparts);
+typedef struct {
+    part_fn fn;
+    void* arg;
+    int part, nparts;
+} part_job;
+static void* part_main(void* p) {
+    part_job* j = (part_job*)p;
+    j->fn(j->arg, j->part, j->nparts);
+    return NULL;
+}
+static void run_parts(part_fn fn, void* arg, int nparts) {
+    if (nparts <= 1) {
+        fn(arg, 0, 1);
+        return;
+    }
+    part_job* jobs = (part_job*)calloc((size_t)nparts, sizeof(part_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nparts, sizeof(pthread_t));
+    for (int k = 0; k < nparts; ++k) {
+        jobs[k].fn = fn;
+        jobs[k].arg = arg;
+        jobs[k].part = k;
+        jobs[k].nparts = nparts;
+        if (k) pthread_create(&th[k], NULL, part_main, &jobs[k]);
+    }
+    fn(arg, 0, nparts);
+    for (int k = 1; k < nparts; ++k) pthread_join(th[k], NULL);
+    free(jobs);
+    free(th);
+}
+static size_t part_lo(size_t n, int part, int nparts) { return n * (size_t)part / (size_t)nparts; }
 
 oracle_ctx* oracle_create(int width, int height, int msaa, float clear_depth) {
     if (width <= 0 || height <= 0 || width > 65535 || height > 65535) return NULL;
@@ -544,10 +586,11 @@ void oracle_log_copy(const oracle_ctx* c, uint32_t* out) {
 /* per-thread accumulation for the row-band parallel pixel loop */
 typedef struct {
     oracle_ctx* c;
-    const rec* recs;
-    size_t nrec;
+    const rec* const* part_recs; /* the block's records, in submission order, in nparts parts */
+    const size_t* part_n;
+    int nparts;
     int fs_id;
-    uint64_t y0, y1;
+    uint64_t band, nbands;
     uint64_t shaded, fsinv, oob;
 } band_job;
 
@@ -591,14 +634,15 @@ static void shade_and_write(oracle_ctx* c, const rec* r, int fs_id, uint64_t x, 
     (*fsinv)++;
 }
 
-/* Per-triangle pixel loop of Rasterizer::rasterize, mod.rs:443-473, over rows [ylo, yhi) */
-static void raster_rec(oracle_ctx* c, const rec* r, int fs_id, uint64_t ylo, uint64_t yhi,
+/* Per-triangle pixel loop of Rasterizer::rasterize, mod.rs:443-473, over the rows of band
+ * `band` of `nbands`: the rows whose 64-row tile row is band modulo nbands (every row when
+ * nbands is 1). Bands share no tile, so they run on separate threads. */
+static void raster_rec(oracle_ctx* c, const rec* r, int fs_id, uint64_t band, uint64_t nbands,
                        uint64_t* shaded, uint64_t* fsinv, uint64_t* oobc) {
     const int S = c->msaa;
     const float(*pat)[2] = S == 4 ? RGSS4 : CENTRE1;
-    uint64_t y0 = r->by0 > ylo ? r->by0 : ylo;
-    uint64_t y1 = r->by1 < yhi ? r->by1 : yhi;
-    for (uint64_t y = y0; y < y1; ++y)
+    for (uint64_t y = r->by0; y < r->by1; ++y) {
+        if (nbands > 1 && (y / TILE_SIZE) % nbands != band) continue;
         for (uint64_t x = r->bx0; x < r->bx1; ++x) {
             float e[4][3];
             unsigned cov = 0;
@@ -625,21 +669,29 @@ static void raster_rec(oracle_ctx* c, const rec* r, int fs_id, uint64_t ylo, uin
             if (!dm) continue;
             shade_and_write(c, r, fs_id, x, y, cov, sd, dm, shaded, fsinv, oobc);
         }
+    }
 }
 
 static void* band_main(void* arg) {
     band_job* j = (band_job*)arg;
-    for (size_t i = 0; i < j->nrec; ++i)
-        raster_rec(j->c, &j->recs[i], j->fs_id, j->y0, j->y1, &j->shaded, &j->fsinv, &j->oob);
+    /* counted in locals: the jobs of neighbouring bands share cache lines */
+    uint64_t shaded = 0, fsinv = 0, oob = 0;
+    for (int p = 0; p < j->nparts; ++p)
+        for (size_t i = 0; i < j->part_n[p]; ++i)
+            raster_rec(j->c, &j->part_recs[p][i], j->fs_id, j->band, j->nbands, &shaded, &fsinv, &oob);
+    j->shaded = shaded;
+    j->fsinv = fsinv;
+    j->oob = oob;
     return NULL;
 }
 
 /* Clip + divide + viewport + setup of one assembled triangle (mod.rs:425-441). Appends 0..n-2
  * records. */
-static size_t triangle_records(oracle_ctx* c, const cvert tri[3], uint32_t tri_index, rec* out) {
+static size_t triangle_records(const oracle_ctx* c, const cvert tri[3], uint32_t tri_index, rec* out,
+                               uint32_t* status) {
     cvert poly[ORACLE_MAX_POLY];
     int n = 0;
-    int res = try_clip(tri, poly, &n, &c->status);
+    int res = try_clip(tri, poly, &n, status);
     if (res == 0) return 0;
     const cvert* src = tri;
     if (res == 1) {
@@ -664,6 +716,126 @@ static size_t triangle_records(oracle_ctx* c, const cvert tri[3], uint32_t tri_i
     return k;
 }
 
+/* vertex shader P*V*W*v over a range of vertices (upstream src/main.rs:147-152) */
+typedef struct {
+    const float* pos;
+    const float* mvp;
+    float* clip;
+    uint32_t nverts;
+} vs_job;
+static void vs_part(void* a, int part, int nparts) {
+    vs_job* j = (vs_job*)a;
+    size_t v0 = part_lo(j->nverts, part, nparts), v1 = part_lo(j->nverts, part + 1, nparts);
+    for (size_t v = v0; v < v1; ++v) {
+        float p4[4] = {j->pos[3 * v], j->pos[3 * v + 1], j->pos[3 * v + 2], 1.0f};
+        oracle_kat_mat4_vec(j->mvp, p4, &j->clip[4 * v]);
+    }
+}
+
+/* primitive assembly + clip/setup (render.rs:75-96, mod.rs:425-441) of a range of triangles
+ * into that range's own record area, in submission order */
+typedef struct {
+    const oracle_ctx* c;
+    const float* clip;
+    const float* uv;
+    const float* rgba;
+    const uint32_t* idx;
+    size_t t0, t1;
+    rec* recs;       /* record area of triangle t0 + k starts at recs + k * maxper */
+    size_t maxper;
+    rec** part_recs;
+    size_t* part_n;
+    uint32_t* part_status;
+} setup_job;
+static void setup_part(void* a, int part, int nparts) {
+    setup_job* j = (setup_job*)a;
+    size_t n = j->t1 - j->t0;
+    size_t lo = part_lo(n, part, nparts), hi = part_lo(n, part + 1, nparts);
+    rec* out = j->recs + lo * j->maxper;
+    size_t k = 0;
+    uint32_t status = 0;
+    for (size_t t = j->t0 + lo; t < j->t0 + hi; ++t) {
+        cvert tri[3];
+        for (int q = 0; q < 3; ++q) {
+            uint32_t vi = j->idx[3 * t + (size_t)q];
+            memcpy(tri[q].p, &j->clip[4 * (size_t)vi], 4 * sizeof(float));
+            if (j->rgba)
+                memcpy(tri[q].a, &j->rgba[4 * (size_t)vi], 4 * sizeof(float));
+            else
+                tri[q].a[0] = tri[q].a[1] = tri[q].a[2] = tri[q].a[3] = 0.0f;
+            tri[q].a[4] = j->uv[2 * (size_t)vi];
+            tri[q].a[5] = j->uv[2 * (size_t)vi + 1];
+        }
+        k += triangle_records(j->c, tri, (uint32_t)(j->c->tri_base + t), &out[k], &status);
+    }
+    j->part_recs[part] = out;
+    j->part_n[part] = k;
+    j->part_status[part] = status;
+}
+
+/* One draw's pixel work on a pool of threads created once per draw: per block of triangles,
+ * every thread clips and sets up its part of the block, then (after a barrier) rasterizes its
+ * band of rows over all the block's records in submission order. */
+/* Sense-reversing barrier that spins (yielding now and then): the pool's threads meet twice
+ * per block, and a sleeping barrier's wake-up latency would dominate small blocks. */
+typedef struct {
+    atomic_int count;
+    atomic_int sense;
+    int n;
+} spin_barrier;
+static void spin_barrier_wait(spin_barrier* b, int* local_sense) {
+    const int s = !*local_sense;
+    *local_sense = s;
+    if (atomic_fetch_add(&b->count, 1) == b->n - 1) {
+        atomic_store(&b->count, 0);
+        atomic_store(&b->sense, s);
+    } else {
+        for (unsigned spins = 0; atomic_load(&b->sense) != s; ++spins)
+            if ((spins & 1023u) == 1023u) sched_yield();
+    }
+}
+
+typedef struct {
+    oracle_ctx* c;
+    setup_job* sj;       /* the block's setup (t0, t1 set per block) */
+    size_t ntris, block;
+    int nthreads, nbands, fs_id;
+    spin_barrier bar;
+} draw_pool;
+typedef struct {
+    draw_pool* pool;
+    int k;
+    uint64_t shaded, fsinv, oob;
+} draw_worker;
+static void* draw_worker_main(void* arg) {
+    draw_worker* w = (draw_worker*)arg;
+    draw_pool* P = w->pool;
+    int sense = 0;
+    for (size_t t0 = 0; t0 < P->ntris; t0 += P->block) {
+        const size_t t1 = t0 + P->block < P->ntris ? t0 + P->block : P->ntris;
+        const int nparts = (t1 - t0) >= 4096u ? P->nthreads : 1;
+        if (w->k < nparts) {
+            setup_job j = *P->sj;
+            j.t0 = t0;
+            j.t1 = t1;
+            setup_part(&j, w->k, nparts);
+        }
+        spin_barrier_wait(&P->bar, &sense);
+        if (w->k < P->nbands) {
+            band_job b = {P->c, (const rec* const*)P->sj->part_recs, P->sj->part_n, nparts, P->fs_id,
+                          (uint64_t)w->k, (uint64_t)P->nbands, 0, 0, 0};
+            band_main(&b);
+            w->shaded += b.shaded;
+            w->fsinv += b.fsinv;
+            w->oob += b.oob;
+        }
+        if (w->k == 0)
+            for (int p = 0; p < nparts; ++p) P->c->status |= P->sj->part_status[p];
+        spin_barrier_wait(&P->bar, &sense);
+    }
+    return NULL;
+}
+
 uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const float* rgba,
                      uint32_t nverts, const uint32_t* idx, uint32_t ntris, const float world[16],
                      const float view[16], const float proj[16], int fs_id, int nthreads) {
@@ -675,69 +847,70 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
         if (idx[i] >= nverts) return ORACLE_INVALID_ARG;
     if (c->log) nthreads = 1;
     if (nthreads < 1) nthreads = 1;
+    c->nthreads = nthreads;
 
     /* vertex shader P*V*W*v, left-associative (upstream src/main.rs:147-152) */
     float pv[16], mvp[16];
     oracle_kat_mat4_mul(proj, view, pv);
     oracle_kat_mat4_mul(pv, world, mvp);
     float* clip = (float*)malloc(sizeof(float) * 4 * (size_t)(nverts ? nverts : 1));
-    for (uint32_t v = 0; v < nverts; ++v) {
-        float p4[4] = {pos[3 * (size_t)v], pos[3 * (size_t)v + 1], pos[3 * (size_t)v + 2], 1.0f};
-        oracle_kat_mat4_vec(mvp, p4, &clip[4 * (size_t)v]);
+    {
+        vs_job vj = {pos, mvp, clip, nverts};
+        run_parts(vs_part, &vj, nverts >= 65536u ? nthreads : 1);
     }
 
     const size_t BLOCK = 1u << 16;
     const size_t maxper = ORACLE_MAX_POLY - 2;
     rec* recs = (rec*)malloc(sizeof(rec) * BLOCK * maxper);
+    rec** part_recs = (rec**)calloc((size_t)nthreads, sizeof(rec*));
+    size_t* part_n = (size_t*)calloc((size_t)nthreads, sizeof(size_t));
+    uint32_t* part_status = (uint32_t*)calloc((size_t)nthreads, sizeof(uint32_t));
+    setup_job sj = {c, clip, uv, rgba, idx, 0, 0, recs, maxper, part_recs, part_n, part_status};
     uint64_t shaded = 0, fsinv = 0, oob = 0;
-    for (size_t t0 = 0; t0 < ntris; t0 += BLOCK) {
-        size_t t1 = t0 + BLOCK < ntris ? t0 + BLOCK : ntris;
-        size_t nrec = 0;
-        for (size_t t = t0; t < t1; ++t) {
-            cvert tri[3];
-            for (int q = 0; q < 3; ++q) {
-                uint32_t vi = idx[3 * t + (size_t)q];
-                memcpy(tri[q].p, &clip[4 * (size_t)vi], 4 * sizeof(float));
-                if (rgba)
-                    memcpy(tri[q].a, &rgba[4 * (size_t)vi], 4 * sizeof(float));
-                else
-                    tri[q].a[0] = tri[q].a[1] = tri[q].a[2] = tri[q].a[3] = 0.0f;
-                tri[q].a[4] = uv[2 * (size_t)vi];
-                tri[q].a[5] = uv[2 * (size_t)vi + 1];
-            }
-            nrec += triangle_records(c, tri, (uint32_t)(c->tri_base + t), &recs[nrec]);
+    if (nthreads == 1) {
+        for (size_t t0 = 0; t0 < ntris; t0 += BLOCK) {
+            sj.t0 = t0;
+            sj.t1 = t0 + BLOCK < ntris ? t0 + BLOCK : ntris;
+            setup_part(&sj, 0, 1);
+            c->status |= part_status[0];
+            for (size_t i = 0; i < part_n[0]; ++i)
+                raster_rec(c, &part_recs[0][i], fs_id, 0, 1, &shaded, &fsinv, &oob);
         }
-        if (nthreads == 1) {
-            for (size_t i = 0; i < nrec; ++i)
-                raster_rec(c, &recs[i], fs_id, 0, (uint64_t)c->h, &shaded, &fsinv, &oob);
-        } else {
-            /* row bands aligned to the 64-row tile grid so no two threads mark one tile */
-            int nb = nthreads;
-            uint64_t rows_tiles = ((uint64_t)c->h + TILE_SIZE - 1) / TILE_SIZE;
-            if ((uint64_t)nb > rows_tiles) nb = (int)rows_tiles;
-            band_job* jobs = (band_job*)calloc((size_t)nb, sizeof(band_job));
-            pthread_t* th = (pthread_t*)calloc((size_t)nb, sizeof(pthread_t));
-            for (int b = 0; b < nb; ++b) {
-                uint64_t ta = rows_tiles * (uint64_t)b / (uint64_t)nb;
-                uint64_t tb = rows_tiles * (uint64_t)(b + 1) / (uint64_t)nb;
-                jobs[b].c = c;
-                jobs[b].recs = recs;
-                jobs[b].nrec = nrec;
-                jobs[b].fs_id = fs_id;
-                jobs[b].y0 = ta * TILE_SIZE;
-                jobs[b].y1 = tb * TILE_SIZE < (uint64_t)c->h ? tb * TILE_SIZE : (uint64_t)c->h;
-                pthread_create(&th[b], NULL, band_main, &jobs[b]);
-            }
-            for (int b = 0; b < nb; ++b) {
-                pthread_join(th[b], NULL);
-                shaded += jobs[b].shaded;
-                fsinv += jobs[b].fsinv;
-                oob += jobs[b].oob;
-            }
-            free(jobs);
-            free(th);
+    } else {
+        /* bands of interleaved 64-row tile rows (row r to band r % nb): no two threads mark one
+         * tile, and uneven scenes spread over every band */
+        const uint64_t rows_tiles = ((uint64_t)c->h + TILE_SIZE - 1) / TILE_SIZE;
+        draw_pool P;
+        P.c = c;
+        P.sj = &sj;
+        P.ntris = ntris;
+        P.block = BLOCK;
+        P.nthreads = nthreads;
+        P.nbands = (uint64_t)nthreads > rows_tiles ? (int)rows_tiles : nthreads;
+        P.fs_id = fs_id;
+        atomic_init(&P.bar.count, 0);
+        atomic_init(&P.bar.sense, 0);
+        P.bar.n = nthreads;
+        draw_worker* ws = (draw_worker*)calloc((size_t)nthreads, sizeof(draw_worker));
+        pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+        for (int k = 0; k < nthreads; ++k) {
+            ws[k].pool = &P;
+            ws[k].k = k;
+            if (k) pthread_create(&th[k], NULL, draw_worker_main, &ws[k]);
         }
+        draw_worker_main(&ws[0]);
+        for (int k = 1; k < nthreads; ++k) pthread_join(th[k], NULL);
+        for (int k = 0; k < nthreads; ++k) {
+            shaded += ws[k].shaded;
+            fsinv += ws[k].fsinv;
+            oob += ws[k].oob;
+        }
+        free(ws);
+        free(th);
     }
+    free(part_recs);
+    free(part_n);
+    free(part_status);
     free(recs);
     free(clip);
     c->tri_base += ntris;
@@ -748,18 +921,25 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
     return ORACLE_OK;
 }
 
-/* Rasterizer::resolve_and_clear, src/rasterizer/mod.rs:478-518 */
-uint32_t oracle_framebuffer(oracle_ctx* c, uint32_t* argb_out) {
+/* Rasterizer::resolve_and_clear, src/rasterizer/mod.rs:478-518, over a range of tiles (the
+ * tiles are disjoint, so ranges run on separate threads) */
+typedef struct {
+    oracle_ctx* c;
+    int prev;
+} resolve_job;
+static void resolve_part(void* a, int part, int nparts) {
+    resolve_job* j = (resolve_job*)a;
+    oracle_ctx* c = j->c;
     const int S = c->msaa;
     oracle_tiles* t = c->tiles;
-    int prev = (t->mask_idx + 1) % 2;
-    for (int i = 0; i < t->n; ++i) {
-        if (!t->mask[prev][i]) continue;
+    int i0 = (int)part_lo((size_t)t->n, part, nparts), i1 = (int)part_lo((size_t)t->n, part + 1, nparts);
+    for (int i = i0; i < i1; ++i) {
+        if (!t->mask[j->prev][i]) continue;
         for (uint64_t y = t->rect[4 * i + 2]; y < t->rect[4 * i + 3]; ++y)
             for (uint64_t x = t->rect[4 * i]; x < t->rect[4 * i + 1]; ++x)
                 c->resolve[y * (uint64_t)c->w + x] = CLEAR_COLOR;
     }
-    for (int i = 0; i < t->n; ++i) {
+    for (int i = i0; i < i1; ++i) {
         if (!t->mask[t->mask_idx][i]) continue;
         for (uint64_t y = t->rect[4 * i + 2]; y < t->rect[4 * i + 3]; ++y)
             for (uint64_t x = t->rect[4 * i]; x < t->rect[4 * i + 1]; ++x) {
@@ -771,6 +951,12 @@ uint32_t oracle_framebuffer(oracle_ctx* c, uint32_t* argb_out) {
                 }
             }
     }
+}
+
+uint32_t oracle_framebuffer(oracle_ctx* c, uint32_t* argb_out) {
+    oracle_tiles* t = c->tiles;
+    resolve_job rj = {c, (t->mask_idx + 1) % 2};
+    run_parts(resolve_part, &rj, c->nthreads > 1 && t->n >= 64 ? c->nthreads : 1);
     oracle_tiles_next(t);
     if (argb_out) memcpy(argb_out, c->resolve, (size_t)c->w * (size_t)c->h * sizeof(uint32_t));
     uint32_t st = c->status;

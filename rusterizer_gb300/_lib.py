@@ -33,6 +33,7 @@ SIGNATURES = {
     "rast_destroy": (None, [_vp]),
     "rast_set_clear_depth": (_i, [_vp, _c.c_float]),
     "rast_set_tile_size": (_i, [_vp, _i]),
+    "rast_set_heavy_tile_entries": (_i, [_vp, _u32]),
     "rast_mesh_upload": (_i, [_vp, _fp, _fp, _fp, _u32, _u32p, _u32, _u32p]),
     "rast_mesh_free": (_i, [_vp, _u32]),
     "rast_mesh_update": (_i, [_vp, _u32, _fp, _fp, _fp, _u32p]),

@@ -247,7 +247,7 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
         }
         int group = 0;
         for (size_t i = 0; i < frames.size() && err == cudaSuccess; ++group) {
-            if (group >= 8) {
+            if (group >= kMaxRasterGroups) {
                 err = cudaErrorInvalidValue;
                 break;
             }
@@ -262,7 +262,8 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
             a.raster_nframes = (int)(j - i);
             a.raster_tile_offset = frames[i].tile_begin;
             a.raster_blocks = blocks;
-            a.raster_queue = &E.d_state->queue[4 * group];
+            a.raster_queue = &E.d_state->queue[kQueueSlots * group];
+            a.raster_heavy_bits = E.heavy_bits;
             err = launch_raster(a, frames[i].msaa, frames[i].ts);
             i = j;
         }
@@ -377,6 +378,14 @@ void rast_destroy(rast_ctx* c) {
 rast_status rast_set_clear_depth(rast_ctx* c, float d) {
     if (!c) return RAST_INVALID_ARG;
     c->clear_depth = d;
+    return RAST_OK;
+}
+
+rast_status rast_set_heavy_tile_entries(rast_ctx* c, uint32_t min_entries) {
+    if (!c) return RAST_INVALID_ARG;
+    // a power of two: bins with at least 2^bits entries are heavy
+    c->E.heavy_bits = min_entries ? 31u - (uint32_t)__builtin_clz(min_entries) : 0u;
+    if (min_entries == 0xFFFFFFFFu) c->E.heavy_bits = 32u;
     return RAST_OK;
 }
 

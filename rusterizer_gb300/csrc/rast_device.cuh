@@ -157,6 +157,10 @@ __device__ __forceinline__ void tri_setup(TriSetup& t, const float4 s[3]) {
 
 // PixelBoundingBox::from (src/rasterizer/bounding_box.rs:13-41) clamped to the viewport
 // (Rasterizer::bounding_box, src/rasterizer/mod.rs:347-361). Half-open [x0,x1) x [y0,y1).
+// The reference converts with `as usize` (64-bit saturation) and then clamps to the viewport;
+// converting with 32-bit saturation gives the same clamped result for any viewport below 2^32:
+// both conversions agree below 2^32, and at or above it both results exceed the viewport and
+// are clamped to it (NaN and negatives give 0 either way).
 __device__ __forceinline__ void pixel_bbox(const float4 s[3], uint32_t width, uint32_t height,
                                            uint32_t& x0, uint32_t& x1, uint32_t& y0,
                                            uint32_t& y1) {
@@ -168,16 +172,10 @@ __device__ __forceinline__ void pixel_bbox(const float4 s[3], uint32_t width, ui
         mny = fminf(mny, s[k].y);
         mxy = fmaxf(mxy, s[k].y);
     }
-    uint64_t a = sat_u64(floorf(mnx)), b = sat_u64(ceilf(mxx));
-    uint64_t c = sat_u64(floorf(mny)), d = sat_u64(ceilf(mxy));
-    if (b > width) b = width;
-    if (d > height) d = height;
-    if (a > width) a = width;
-    if (c > height) c = height;
-    x0 = (uint32_t)a;
-    x1 = (uint32_t)b;
-    y0 = (uint32_t)c;
-    y1 = (uint32_t)d;
+    x0 = min(sat_u32(floorf(mnx)), width);
+    x1 = min(sat_u32(ceilf(mxx)), width);
+    y0 = min(sat_u32(floorf(mny)), height);
+    y1 = min(sat_u32(ceilf(mxy)), height);
 }
 
 // EdgeFunctions::eval_single (src/rasterizer/mod.rs:125-132): normal . (p - point), dot

@@ -176,7 +176,7 @@ struct DeviceState {
     unsigned long long log_n;
     unsigned int clip_n;     // triangles queued for the warp clipper
     unsigned int pad2;
-    unsigned int queue[32];  // raster tile queues, 4 counters per (msaa, tile) group
+    unsigned int queue[kQueueSlots * kMaxRasterGroups];  // raster tile queues per (msaa, tile) group
 };
 
 struct Engine {
@@ -195,6 +195,7 @@ struct Engine {
     DeviceState* d_state = nullptr;
     DeviceState* h_state = nullptr;
     uint64_t clip_hint = 0;
+    uint32_t heavy_bits = kDefaultHeavyBits;  // bins of >= 2^heavy_bits entries: CTA-wide raster
     bool sync_after = true;
     bool profiling = false;
     cudaEvent_t ev[6] = {};

@@ -344,17 +344,20 @@ __global__ void __launch_bounds__(256) k_clip(const DrawDev* __restrict__ draws,
 
 // ===================================================================== binning: count
 
-__global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ chunks,
+__global__ void __launch_bounds__(256, 8) k_bin_count(const ChunkDev* __restrict__ chunks,
                                                    const DrawDev* __restrict__ draws,
                                                    const FrameDev* __restrict__ frames,
                                                    Scratch s) {
     pdl_enter();
+    // per-bin counts of the chunk, two 16-bit counters per word (bin t in half t & 1 of word
+    // t / 2): a chunk holds at most 8192 triangles, so no counter carries into its neighbour,
+    // and the histogram of 16384 bins takes 32 KB (8 CTAs per SM for the largest frames)
     extern __shared__ uint32_t hist[];
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
     const FrameDev& f = frames[d.frame];
     const uint32_t nt = f.ntiles, tx = f.tiles_x;
-    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) hist[t] = 0;
+    for (uint32_t t = threadIdx.x; t < (nt + 1) / 2; t += blockDim.x) hist[t] = 0;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < ch.tri_count; i += blockDim.x) {
         const uint32_t tri = ch.tri_begin + i;
@@ -368,12 +371,15 @@ __global__ void __launch_bounds__(256) k_bin_count(const ChunkDev* __restrict__ 
             uint32_t x0, y0, x1, y1;
             tile_rect(rect, (uint32_t)f.ts, x0, y0, x1, y1);
             for (uint32_t y = y0; y <= y1; ++y)
-                for (uint32_t x = x0; x <= x1; ++x) atomicAdd(&hist[y * tx + x], 1u);
+                for (uint32_t x = x0; x <= x1; ++x) {
+                    const uint32_t t = y * tx + x;
+                    atomicAdd(&hist[t >> 1], (t & 1u) ? 0x10000u : 1u);
+                }
         }
     }
     __syncthreads();
     uint32_t* row = s.counts + f.count_base + (unsigned long long)ch.row * nt;
-    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) row[t] = hist[t];
+    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) row[t] = (hist[t >> 1] >> ((t & 1u) * 16u)) & 0xFFFFu;
 }
 
 // ===================================================================== binning: scans
@@ -682,8 +688,9 @@ __global__ void __launch_bounds__(kScatterThreads) k_bin_scatter(
 
 // ===================================================================== raster
 
-constexpr int kRasterThreads = 256;
+constexpr int kRasterThreads = 128;
 constexpr int kRasterWarps = kRasterThreads / 32;
+constexpr int kRasterCtasPerSm = 7;  // occupancy the launch bounds aim at (shared memory allows 7)
 constexpr int kEmptyRun = 8;  // bins without entries taken per queue update
 constexpr uint32_t kTrimMin = 4;  // shortest box line that line_span trims
 
@@ -696,7 +703,8 @@ struct RasterCfg {
     static constexpr int IC = kRasterThreads;  // items (triangles after clipping) per batch
     static constexpr int QC = 64;              // per-warp fragment ring
     static_assert(TS <= 16 && IC <= 256, "ring entries hold item and pixel in one byte each");
-    static_assert(TS <= 2 * kRasterWarps, "row mode gives a warp at most two rows of a tile");
+    static constexpr int LINES = (TS + kRasterWarps - 1) / kRasterWarps;  // lines of a tile per warp
+    static_assert(LINES <= 4, "an item meets a warp on at most four lines of a tile");
 };
 
 template <int S, int TS>
@@ -755,8 +763,8 @@ __device__ __forceinline__ uint32_t frame_of_tile(const FrameDev* __restrict__ f
 
 // Inward edge normal k of an item (RasterizerTriangle::new, src/rasterizer/mod.rs:199-204),
 // recomputed from the stored points with the same two subtractions.
-template <int S, int TS>
-__device__ __forceinline__ void item_normal(const RasterSmem<S, TS>& sm, uint32_t it, int k, float& nx,
+template <typename SM>
+__device__ __forceinline__ void item_normal(const SM& sm, uint32_t it, int k, float& nx,
                                             float& ny) {
     const int n = k == 2 ? 0 : k + 1;
     const float vx = sm.ipx[n][it] - sm.ipx[k][it];
@@ -790,8 +798,8 @@ __device__ __forceinline__ float edge_room(float nx, float ny, float Px, float P
 // computed in f32 to within 0.03 pixel whenever it falls near the tile (|pal - gk / nal| below
 // 2^16; farther out only its sign matters), and the interval is widened by 1/8 pixel.
 // Non-finite points are not trimmed.
-template <int S, int TS>
-__device__ __forceinline__ void line_span(const RasterSmem<S, TS>& sm, uint32_t it, uint32_t mode, uint32_t lc,
+template <int S, int TS, typename SM>
+__device__ __forceinline__ void line_span(const SM& sm, uint32_t it, uint32_t mode, uint32_t lc,
                                           uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
     const float px[3] = {sm.ipx[0][it], sm.ipx[1][it], sm.ipx[2][it]};
     const float py[3] = {sm.ipy[0][it], sm.ipy[1][it], sm.ipy[2][it]};
@@ -1154,15 +1162,16 @@ __device__ __forceinline__ void clear_tile_warp(const FrameDev& f, uint32_t x0, 
     }
 }
 
-// Persistent raster kernel. Units are (bin with entries, quadrant) pairs taken heaviest bin
-// first from queue[0]; per unit the CTA replays the bin in submission order in batches of up
-// to IC items: stage the items (A), split the tile's rows or columns over the warps by work
+// Persistent raster kernel for the heavy tiles. Units are (bin, quadrant) pairs of the first
+// queue[3] bins of the raster queue (the bins with the most entries; the others go one warp per
+// tile to k_raster_warp), taken heaviest bin first from queue[0]; per unit the CTA replays the
+// bin in submission order in batches of up to IC items: stage the items (A), split the tile's rows or columns over the warps by work
 // (B), then each warp walks the candidate pixels of its items inside its range — coverage
 // (EdgeFunctions::eval, mod.rs:134-146) and sample depths (RasterizerTriangle::fragment,
 // mod.rs:225-253) — and depth-tests, shades and writes the covered fragments in order (C).
 // Bins without entries are then cleared by single warps from queue[1].
 template <int S, int TS>
-__global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __restrict__ frames,
+__global__ void __launch_bounds__(kRasterThreads, kRasterCtasPerSm) k_raster(const FrameDev* __restrict__ frames,
                                                            int nframes,
                                                            const uint32_t* __restrict__ order,
                                                            uint32_t ntotal, uint32_t nsx,
@@ -1174,9 +1183,10 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterSmem<S, TS>& sm = *reinterpret_cast<RasterSmem<S, TS>*>(smem_raw);
     const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-    sm.inv255[threadIdx.x] = (float)threadIdx.x / 255.0f;  // blockDim.x == 256
+    for (uint32_t b = threadIdx.x; b < 256u; b += blockDim.x) sm.inv255[b] = (float)b / 255.0f;
     uint32_t shaded = 0, fsinv = 0, oobc = 0;
     const uint32_t nbusy = *(volatile unsigned int*)&queue[2];  // written by k_tile_order
+    const uint32_t nheavy = *(volatile unsigned int*)&queue[3];  // the first nheavy bins of the queue
     const uint32_t nsub = nsx * nsx;
 
     // unit tickets (heaviest first); the next one is taken when the current unit starts its
@@ -1186,7 +1196,7 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     __syncthreads();
     // misc[0] is written again only after this unit's resolve, many barriers later
     const uint32_t qi = sm.misc[0];
-    if (qi >= nbusy * nsub) break;
+    if (qi >= nheavy * nsub) break;
     const uint32_t gt = order[qi / nsub], sub = qi % nsub;
     const FrameDev& f = frames[frame_of_tile(frames, nframes, gt)];
     const uint32_t lt = gt - f.tile_begin;
@@ -1311,10 +1321,11 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
             const bool act = gb + lane < nmine;
             const uint32_t it_l = act ? sm.wlist[warp][gb + lane] : 0u;
             // candidates of the lane's item: its lines owned by this warp (rows, or columns in
-            // column mode: the first, then first + kRasterWarps), each trimmed by line_span;
-            // geo = first line | first-line start << 5 | first-line length << 10 |
-            // second-line start << 15
-            uint32_t c = 0, geo = 0;
+            // column mode: first, first + kRasterWarps, ... up to C::LINES of them), each
+            // trimmed by line_span; geo = first line | start 1 << 5 | length 1 << 10 |
+            // start 2 << 15 | length 2 << 20 | start 3 << 25, geo2 = length 3 | start 4 << 5
+            // (the fourth length is what remains of the count)
+            uint32_t c = 0, geo = 0, geo2 = 0;
             if (act) {
                 const uint32_t r = sm.irect[it_l];
                 const uint32_t lx0 = r & 0xFFu, ly0 = (r >> 8) & 0xFFu, lx1 = (r >> 16) & 0xFFu, ly1 = r >> 24;
@@ -1322,24 +1333,26 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 const uint32_t b0 = mode ? ly0 : lx0, b1 = mode ? ly1 : lx1;  // along each line
                 const uint32_t first = l0 + ((warp + kRasterWarps - (l0 % kRasterWarps)) % kRasterWarps);
                 const uint32_t nlines = first < l1 ? (l1 - first + kRasterWarps - 1) / kRasterWarps : 0u;
-                uint32_t s1 = b0, e1 = b1, s2 = b0, e2 = b1;
+                uint32_t sa[4] = {b0, b0, b0, b0}, ea[4] = {b1, b1, b1, b1};
                 // lines shorter than kTrimMin pixels are cheaper to test whole than to trim
                 const uint32_t ntrim = b1 - b0 >= kTrimMin ? nlines : 0u;
 #pragma unroll 1
                 for (uint32_t ln = 0; ln < ntrim; ++ln) {
                     uint32_t a0 = b0, a1 = b1;
                     line_span<S, TS>(sm, it_l, mode, first + ln * kRasterWarps, X0, Y0, a0, a1);
-                    if (ln == 0) {
-                        s1 = a0;
-                        e1 = a1;
-                    } else {
-                        s2 = a0;
-                        e2 = a1;
+                    // selects, not an indexed store (the arrays stay in registers)
+#pragma unroll
+                    for (uint32_t q = 0; q < (uint32_t)C::LINES; ++q) {
+                        sa[q] = ln == q ? a0 : sa[q];
+                        ea[q] = ln == q ? a1 : ea[q];
                     }
                 }
-                const uint32_t w1 = nlines > 0 ? e1 - s1 : 0u, w2 = nlines > 1 ? e2 - s2 : 0u;
-                c = w1 + w2;
-                geo = first | (s1 << 5) | (w1 << 10) | (s2 << 15);
+                uint32_t w[4];
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) w[q] = nlines > q ? ea[q] - sa[q] : 0u;
+                c = w[0] + w[1] + w[2] + w[3];
+                geo = first | (sa[0] << 5) | (w[0] << 10) | (sa[1] << 15) | (w[1] << 20) | (sa[2] << 25);
+                geo2 = w[2] | (sa[3] << 5);
             }
             uint32_t incl = c;
 #pragma unroll
@@ -1361,16 +1374,24 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
                 const uint32_t it = __shfl_sync(0xFFFFFFFFu, it_l, sj);
                 const uint32_t exc = __shfl_sync(0xFFFFFFFFu, incl - c, sj);
                 const uint32_t gg = __shfl_sync(0xFFFFFFFFu, geo, sj);
+                const uint32_t gg2 = C::LINES > 2 ? __shfl_sync(0xFFFFFFFFu, geo2, sj) : 0u;
                 uint32_t cov = 0, pix = 0;
                 float z[S];
 #pragma unroll
                 for (int k = 0; k < S; ++k) z[k] = 0.0f;
                 if (p < total) {
                     const uint32_t rr = p - exc;
-                    const uint32_t w1 = (gg >> 10) & 31u;
-                    const bool second = rr >= w1;
-                    const uint32_t along = second ? ((gg >> 15) & 31u) + (rr - w1) : ((gg >> 5) & 31u) + rr;
-                    const uint32_t line = (gg & 31u) + (second ? (uint32_t)kRasterWarps : 0u);
+                    // which of the item's lines: cumulative lengths c1 <= c2 <= c3
+                    const uint32_t c1 = (gg >> 10) & 31u, c2 = c1 + ((gg >> 20) & 31u), c3 = c2 + (gg2 & 31u);
+                    uint32_t k = (uint32_t)(rr >= c1);
+                    uint32_t start = k ? (gg >> 15) & 31u : (gg >> 5) & 31u, base = k ? c1 : 0u;
+                    if (C::LINES > 2) {
+                        start = rr >= c2 ? (rr >= c3 ? (gg2 >> 5) & 31u : gg >> 25) : start;
+                        base = rr >= c2 ? (rr >= c3 ? c3 : c2) : base;
+                        k += (uint32_t)(rr >= c2) + (uint32_t)(rr >= c3);
+                    }
+                    const uint32_t along = start + (rr - base);
+                    const uint32_t line = (gg & 31u) + k * (uint32_t)kRasterWarps;
                     const uint32_t lx = mode ? line : along, ly = mode ? along : line;
                     pix = ly * TS + lx;
                     const float fx = (float)(X0 + lx), fy = (float)(Y0 + ly);
@@ -1489,6 +1510,8 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(const FrameDev* __
     }
 }
 
+#include "rast_raster_warp.cuh"
+
 // Splits each 32-pixel bin with entries into its four quadrant lists, keeping submission
 // order within each (an entry goes to every quadrant its mask names). Persistent CTAs walk the
 // bins with entries in the raster queue's order (k_tile_order runs first); the quadrant raster
@@ -1576,13 +1599,15 @@ __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ 
 }
 
 // Tile queue of one raster launch: tiles with entries first, in decreasing order of entry
-// count (bucketed by bit length), then tiles without entries; queue[2] = tiles with entries.
-// One block.
+// count (bucketed by bit length), then tiles without entries; queue[2] = tiles with entries,
+// queue[3] = the leading tiles with at least 2^heavy_bits entries (rastered CTA-wide by
+// k_raster; the rest one warp per tile by k_raster_warp). One block.
 __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
                                                      const uint32_t* __restrict__ tile_count,
                                                      uint32_t* __restrict__ order,
                                                      unsigned int* __restrict__ queue,
-                                                     const uint32_t* __restrict__ status) {
+                                                     const uint32_t* __restrict__ status,
+                                                     uint32_t heavy_bits) {
     pdl_enter();
     __shared__ uint32_t cnt[33], off[33];
     if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
@@ -1598,12 +1623,15 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t run = 0;
+        uint32_t run = 0, heavy = 0;
         for (int b = 32; b >= 0; --b) {
             off[b] = run;
             run += cnt[b];
+            // bins of at least 2^heavy_bits entries (bit length above heavy_bits), never empty ones
+            if (b > (int)heavy_bits && b > 0) heavy += cnt[b];
         }
         queue[2] = n - cnt[0];
+        queue[3] = heavy;
     }
     __syncthreads();
     for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
@@ -1666,28 +1694,38 @@ static int sm_count() {
     return n;
 }
 
+// Persistent grid of a kernel on the current device: resident CTAs per SM x SMs, with its
+// dynamic shared-memory limit raised to `bytes` (done once per device and kernel; every host
+// thread computes the same).
+template <typename K>
+static cudaError_t persistent_grid(K kernel, int threads, size_t bytes, std::atomic<int>* cache, int& grid) {
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    grid = cache[dev].load(std::memory_order_acquire);
+    if (grid) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    int per = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, bytes);
+    if (e != cudaSuccess) return e;
+    grid = (per > 0 ? per : 1) * sm_count();
+    cache[dev].store(grid, std::memory_order_release);
+    return cudaSuccess;
+}
+
 template <int S, int TS>
 static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     const size_t bytes = sizeof(RasterSmem<S, TS>);
-    // persistent grid: resident CTAs per SM x SMs, set up once per device (every thread
-    // computes the same)
-    static std::atomic<int> grid_cap_once[kMaxDevices];
-    const int dev = current_device();
-    if (dev < 0) return cudaErrorInvalidDevice;
-    int grid_cap = grid_cap_once[dev].load(std::memory_order_acquire);
-    if (!grid_cap) {
-        cudaError_t e = cudaFuncSetAttribute(k_raster<S, TS>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        if (e != cudaSuccess) return e;
-        int per = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster<S, TS>, kRasterThreads, bytes);
-        if (e != cudaSuccess) return e;
-        grid_cap = (per > 0 ? per : 1) * sm_count();
-        grid_cap_once[dev].store(grid_cap, std::memory_order_release);
-    }
+    const size_t wbytes = sizeof(WarpRasterSmem<S, TS>);
+    static std::atomic<int> cta_cap[kMaxDevices], warp_cap[kMaxDevices];
+    int grid_cap = 0, wgrid_cap = 0;
+    cudaError_t e = persistent_grid(k_raster<S, TS>, kRasterThreads, bytes, cta_cap, grid_cap);
+    if (e != cudaSuccess) return e;
+    e = persistent_grid(k_raster_warp<S, TS>, 32 * kWarpUnitWarps, wbytes, warp_cap, wgrid_cap);
+    if (e != cudaSuccess) return e;
     if (a.raster_blocks == 0) return cudaSuccess;
-    cudaError_t e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks,
-                               a.scratch.tile_count, a.scratch.tile_order, a.raster_queue, a.scratch.status);
+    e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
+                   a.scratch.tile_order, a.raster_queue, a.scratch.status, a.raster_heavy_bits);
     if (e != cudaSuccess) return e;
     if (nsx > 1) {
         const unsigned sgrid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
@@ -1697,10 +1735,21 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         if (e != cudaSuccess) return e;
     }
     const unsigned long long units = (unsigned long long)a.raster_blocks * nsx * nsx;
-    const unsigned grid = units < (unsigned long long)grid_cap ? (unsigned)units : (unsigned)grid_cap;
-    return launch_pdl(k_raster<S, TS>, grid, kRasterThreads, bytes, a.stream, a.raster_frames, a.raster_nframes,
-                      (const uint32_t*)(a.scratch.tile_order + a.raster_tile_offset), a.raster_blocks, nsx,
-                      a.raster_queue, a.draws, a.scratch);
+    // heavy tiles CTA-wide (none when every bin is below the threshold: the launch then only
+    // helps with the bins without entries), then the light tiles one warp each
+    if (a.raster_heavy_bits < 32) {
+        const unsigned grid = units < (unsigned long long)grid_cap ? (unsigned)units : (unsigned)grid_cap;
+        e = launch_pdl(k_raster<S, TS>, grid, kRasterThreads, bytes, a.stream, a.raster_frames, a.raster_nframes,
+                       (const uint32_t*)(a.scratch.tile_order + a.raster_tile_offset), a.raster_blocks, nsx,
+                       a.raster_queue, a.draws, a.scratch);
+        if (e != cudaSuccess) return e;
+    }
+    if (a.raster_heavy_bits == 0) return cudaSuccess;  // every bin with entries is heavy
+    const unsigned long long wunits = (units + kWarpUnitWarps - 1) / kWarpUnitWarps;
+    const unsigned wgrid = wunits < (unsigned long long)wgrid_cap ? (unsigned)wunits : (unsigned)wgrid_cap;
+    return launch_pdl(k_raster_warp<S, TS>, wgrid, 32 * kWarpUnitWarps, wbytes, a.stream, a.raster_frames,
+                      a.raster_nframes, (const uint32_t*)(a.scratch.tile_order + a.raster_tile_offset),
+                      a.raster_blocks, nsx, a.raster_queue, a.draws, a.scratch);
 }
 
 cudaError_t launch_vertex(const LaunchArgs& a) {
@@ -1714,7 +1763,7 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
     // smaller value set by another host thread must not undercut a concurrent larger launch
     static std::mutex mu;
     static int configured[kMaxDevices] = {};
-    const int bytes = (int)(a.max_tiles * sizeof(uint32_t));
+    const int bytes = (int)(((a.max_tiles + 1) / 2) * sizeof(uint32_t));
     const int dev = current_device();
     if (dev < 0) return cudaErrorInvalidDevice;
     {

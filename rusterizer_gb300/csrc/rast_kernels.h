@@ -25,7 +25,8 @@ struct LaunchArgs {
     int raster_nframes;
     uint32_t raster_tile_offset;
     uint32_t raster_blocks;        // tiles in the group
-    unsigned int* raster_queue;    // the group's 4 tile-queue counters (zeroed per frame)
+    unsigned int* raster_queue;    // the group's kQueueSlots tile-queue counters (zeroed per frame)
+    uint32_t raster_heavy_bits;    // bins of >= 2^bits entries are rastered CTA-wide (32: none)
     Scratch scratch;
 };
 

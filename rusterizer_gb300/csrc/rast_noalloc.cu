@@ -237,6 +237,7 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
         a.raster_tile_offset = 0;
         a.raster_blocks = F.ntiles;
         a.raster_queue = dstate->queue;
+        a.raster_heavy_bits = kDefaultHeavyBits;
         Scratch& S = a.scratch;
         S.vclip = reinterpret_cast<float4*>(base + L.vclip);
         S.vscr = reinterpret_cast<float4*>(base + L.vscr);

@@ -31,6 +31,13 @@ constexpr int kMaxPoly = 32;                   // clip polygon capacity (a conve
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kRectEmpty = ~0ull;
 constexpr int kMaxTilesPerFrame = 16384;       // per-frame tile count limit (smem histograms)
+// Raster tile queue counters per (msaa, tile) launch group: [0] heavy-tile tickets, [1] empty-bin
+// tickets, [2] bins with entries, [3] heavy bins, [4] light-tile tickets
+constexpr int kQueueSlots = 8;
+constexpr int kMaxRasterGroups = 8;
+// Bins with at least 2^kDefaultHeavyBits entries are rastered CTA-wide, the others one warp per
+// raster tile (rast_set_heavy_tile_entries)
+constexpr uint32_t kDefaultHeavyBits = 0;
 // bin entries: triangle << 5 | clipped << 4 | mask of the raster quadrants the box touches
 constexpr int kEntShift = 5;
 constexpr uint32_t kEntClipped = 1u << 4;
