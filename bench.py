@@ -449,9 +449,11 @@ def run_ours(args):
     for k in range(min(args.steps, args.warmup)):
         frame(k)  # the same loop untimed: warm-up of the asynchronous path
     barrier()
+    n_launch0 = L.rast_kernel_launches()
     for k in range(args.steps):
         step_ms.append(frame(k))
     barrier()
+    timed_launches = int(L.rast_kernel_launches() - n_launch0)
     clk.__exit__(None, None, None)
     # the per-stage split from separate profiled frames (not part of the value)
     r.set_profiling(True)
@@ -563,7 +565,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": W * H * 4, "host_threads": 2,
                     "one_thread_value": e2e_serial},
-            "gpu_launches": launches_per_frame(W, H, scenes.scene_triangles(scene), args.tile) * args.steps,
+            "gpu_launches": timed_launches,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -600,7 +602,10 @@ def run_batched(args):
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
     reps.barrier()
+    # both arms are timed the same way: host wall clock from a synchronised start to the end of
+    # the last scene (the batched arm's CUDA events give the device time beside it)
     with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
         for k in range(args.steps):
             with torch.cuda.stream(ext):
                 evs[k][0].record(ext)
@@ -608,20 +613,32 @@ def run_batched(args):
             with torch.cuda.stream(ext):
                 evs[k][1].record(ext)
         ext.synchronize()
+        batch_wall = time.perf_counter() - t0
         reps.barrier()
     batch_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = reps.max([sum(batch_ms)])[0]
-    value = world * len(sc) * args.steps / (total_ms / 1000.0)
-    # plain: one scene per launch sequence, synchronous, 256 calls
-    for i in range(len(sc)):
-        br.render([ptrs[i]], indices=[i])
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(len(sc)):
-        br.render([ptrs[i]], indices=[i])
-    torch.cuda.synchronize()
-    plain_s = reps.max([time.perf_counter() - t0])[0]
-    plain_value = world * len(sc) / plain_s
+    total_ms, batch_wall = reps.max([sum(batch_ms), batch_wall])
+    value = world * len(sc) * args.steps / batch_wall
+    device_value = world * len(sc) * args.steps / (total_ms / 1000.0)
+    # plain: one scene per launch sequence (the single-scene path: rast_render_batch of one
+    # scene, synchronous with its status check, as rast_framebuffer is), 256 calls; timed with the
+    # batch's tuned raster settings and with the library defaults (every bin CTA-wide: one scene
+    # alone has too few tiles to keep one warp per tile busy), the faster one counts
+    from rusterizer_gb300 import _lib
+    L = _lib.load()
+
+    def plain_rate():
+        for i in range(len(sc)):
+            br.render([ptrs[i]], indices=[i])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(len(sc)):
+            br.render([ptrs[i]], indices=[i])
+        torch.cuda.synchronize()
+        return world * len(sc) / reps.max([time.perf_counter() - t0])[0]
+    plain_tuned = plain_rate()
+    L.rast_set_heavy_tile_entries(br._ctx, 0)
+    plain_default = plain_rate()
+    plain_value = max(plain_tuned, plain_default)
     # e2e: the whole batch through the public API with host outputs (device -> host copies)
     host = [np.empty((s["height"], s["width"]), np.uint32) for s in sc]
     br.render(host)
@@ -645,12 +662,15 @@ def run_batched(args):
     if rank == 0:
         print(json.dumps({
             "metric": "scenes/s", "value": value, "unit": "scenes/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * batch_wall / args.steps,
             "ms_per_step_median": statistics.median(batch_ms),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": batch_config(3, sc, world), "autotune": tuned,
             "plain_scenes_per_s": plain_value, "batched_vs_plain": value / plain_value,
+            "plain_scenes_per_s_tuned": plain_tuned, "plain_scenes_per_s_default": plain_default,
+            "device_scenes_per_s": device_value,
+            "timing": "both arms host wall clock over synchronised runs; device_scenes_per_s from CUDA events",
             "roofline": {"bound": "hbm", "kernel": "whole batch", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": None, "algorithmic_bytes_per_step": bytes_batch},
@@ -713,21 +733,50 @@ def run_serving(args):
     rng = np.random.default_rng(4)
     results = {}
     bound = args.p99_bound_ms
+    L = __import__("rusterizer_gb300._lib", fromlist=["load"]).load()
+    clk = None
     for mode in ("batched", "plain"):
+        if mode == "plain":
+            # one request per launch gains nothing from the warp-per-tile kernel (too few tiles
+            # per launch): the plain server runs every bin CTA-wide, the library default
+            L.rast_set_heavy_tile_entries(br._ctx, 0)
         srv = RenderServer(br, budget_bytes=40 << 30, streams=2, one_per_launch=(mode == "plain"))
         poisson_run(srv, len(sc), outs, 2000.0, 0.5, rng)  # warm-up: sizes every buffer
         sweep = []
+        sampler = ClockSampler(local) if mode == "batched" else None
+        if sampler:
+            sampler.__enter__()
         for rate in args.rates:
+            n0 = L.rast_kernel_launches()
             st = poisson_run(srv, len(sc), outs, rate, args.seconds, rng)
+            st["gpu_launches"] = int(L.rast_kernel_launches() - n0)
             sweep.append(st)
             if st["p99_ms"] > 4 * bound:
                 break
+        if sampler:
+            sampler.__exit__(None, None, None)
+            clk = sampler.summary()
         srv.close()
         ok = [s for s in sweep if s["p99_ms"] <= bound]
         best = max(ok, key=lambda s: s["req_per_s"]) if ok else None
         results[mode] = {"sweep": sweep, "max_rate_within_bound": best["offered_rate"] if best else 0.0,
                          "at_max": best}
     br.close()
+    # algorithmic bytes of the requests served per second at the highest rate within the bound
+    # (requests draw scenes uniformly from the pool)
+    mean_bytes = sum(scenes.scene_bytes(s) for s in sc) / len(sc)
+    peak, peak_kind = measured_peak_gbs()
+    served = (results["batched"]["at_max"] or {}).get("req_per_s", 0.0)
+    achieved = served * mean_bytes / 1e9
+    cpu = None
+    if world == 1 and rank == 0 and args.cpu_seconds > 0:
+        cores = os.cpu_count() or 1
+        rate1, n1, dt1 = scene_mix_rate(sc, 1, args.cpu_seconds)
+        rate_n, n_n, dt_n = scene_mix_rate(sc, cores, args.cpu_seconds)
+        cpu = {"value": rate1, "unit": "requests/s", "cores": 1, "kind": "port",
+               "sample": f"{n1} scenes of the pool, single thread, {dt1:.1f} s of frames",
+               "scene_parallel": {"value": rate_n, "cores": cores,
+                                  "sample": f"{n_n} scenes, one scene per thread, {dt_n:.1f} s of frames"}}
     b, p = results["batched"], results["plain"]
     # replicas serve independent request streams: rates add up, the tail latency is the worst
     at = dict(b["at_max"] or {})
@@ -752,7 +801,13 @@ def run_serving(args):
                           for s in results[m]["sweep"]] for m in results},
             "e2e": {"value": b["max_rate_within_bound"], "unit": "requests/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "roofline": None, "cpu_baseline": None, "gpu_launches": None,
+            "roofline": {"bound": "hbm", "kernel": "requests served at the highest rate within the bound",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_request": mean_bytes},
+            "cpu_baseline": cpu,
+            "gpu_launches": sum(st.get("gpu_launches", 0) for st in b["sweep"]),
+            "clocks": clk,
         }), flush=True)
     return 0
 
@@ -765,7 +820,7 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--nscenes", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+",
-                    default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 10000, 12000, 16000])
+                    default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 12000, 16000, 20000, 24000, 32000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--p99-bound-ms", type=float, default=50.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

@@ -150,8 +150,26 @@ typedef struct rast_scene {
  * per-scene results as rendering each scene alone. Synchronous. */
 rast_status rast_render_batch(rast_ctx* ctx, const rast_scene* scenes, uint32_t n);
 
-/* Times tile sizes 8/16/32 for the MSAA-1 and MSAA-4 scenes of a batch and keeps the fastest
- * pair in the context (used where rast_scene.tile == 0). best_tiles[0] = MSAA 1, [1] = MSAA 4. */
+/* Settings the batch autotuner chooses, per MSAA class ([0] MSAA 1, [1] MSAA 4). */
+typedef struct rast_tuning {
+    int tile[2];                  /* bin edge in pixels: 8, 16 or 32 */
+    uint32_t heavy_entries[2];    /* rast_set_heavy_tile_entries threshold: 0 = every bin CTA-wide,
+                                     0xFFFFFFFF = every bin one warp per tile */
+    int raster_ctas_per_sm[2];    /* persistent raster CTAs per SM, 0 = as many as fit */
+    uint64_t bin_capacity;        /* bin entries reserved for the batch (measured need + 1/8) */
+    float batch_ms;               /* batch time with the chosen settings */
+} rast_tuning;
+
+/* Times the batch under each candidate setting and keeps the fastest in the context (used by
+ * rast_render_batch, rast_batch_create and servers created afterwards, where rast_scene.tile is
+ * 0): first the bin edge 8/16/32 of both MSAA classes together, then per class the raster
+ * kernel split (every bin CTA-wide, bins of 512+ entries CTA-wide, every bin one warp per tile)
+ * with all the raster CTAs that fit, 4 or 2 per SM; finally one run measures each scene's bins
+ * and the batch reserves that plus an eighth. Images are written to scratch, not the scenes'
+ * outputs. No counterpart in the reference (its tile size is the constant TILE_SIZE = 64,
+ * src/rasterizer/buffers.rs:8). */
+rast_status rast_autotune_batch_ex(rast_ctx* ctx, const rast_scene* scenes, uint32_t n, rast_tuning* out);
+/* The same, returning the bin edges only: best_tiles[0] = MSAA 1, [1] = MSAA 4. */
 rast_status rast_autotune_batch(rast_ctx* ctx, const rast_scene* scenes, uint32_t n,
                                 int best_tiles[2]);
 
@@ -210,6 +228,10 @@ rast_status rast_stats(rast_ctx* ctx, uint64_t* shaded_samples, uint64_t* fs_inv
 
 /* The context's CUDA stream (cudaStream_t) for event timing by the caller. */
 void* rast_stream(rast_ctx* ctx);
+/* Pipeline kernels this process has launched through the library so far (every context,
+ * batch and server; a captured batch counts its kernels once, at capture). For throughput
+ * accounting; no counterpart in the reference. */
+uint64_t rast_kernel_launches(void);
 
 /* Stage timing with CUDA events on the context stream. When enabled, rast_stage_times
  * fills up to n floats (ms) of the last frame: vertex, bin-count, scan, scatter, raster. */

@@ -46,6 +46,8 @@ SIGNATURES = {
                                  _fp, _fp, _fp, _vp, _i, _i, _i, _vp, _vp]),
     "rast_render_batch": (_i, [_vp, _vp, _u32]),
     "rast_autotune_batch": (_i, [_vp, _vp, _u32, _c.POINTER(_i)]),
+    "rast_autotune_batch_ex": (_i, [_vp, _vp, _u32, _vp]),
+    "rast_kernel_launches": (_u64, []),
     "rast_batch_create": (_i, [_vp, _vp, _u32, _c.POINTER(_vp)]),
     "rast_batch_launch": (_i, [_vp, _i]),
     "rast_batch_stream": (_vp, [_vp]),
@@ -76,6 +78,12 @@ class Scene(ctypes.Structure):
                 ("clear_depth", _c.c_float), ("mesh", _c.c_uint32), ("texture", _c.c_int),
                 ("fs_id", _c.c_int), ("world", _c.c_float * 16), ("view", _c.c_float * 16),
                 ("proj", _c.c_float * 16), ("argb_out", _c.c_void_p)]
+
+
+class Tuning(ctypes.Structure):
+    """struct rast_tuning (include/rast.h)."""
+    _fields_ = [("tile", _c.c_int * 2), ("heavy_entries", _c.c_uint32 * 2), ("raster_ctas_per_sm", _c.c_int * 2),
+                ("bin_capacity", _c.c_uint64), ("batch_ms", _c.c_float)]
 
 
 class ServerConfig(ctypes.Structure):

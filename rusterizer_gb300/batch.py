@@ -82,13 +82,18 @@ class BatchRenderer:
         return st
 
     def autotune(self, outputs, indices=None, cache=True):
-        """Pick the fastest tile sizes (MSAA 1, MSAA 4) for this batch; cached on disk."""
+        """Pick the fastest settings for this batch (rast_autotune_batch_ex): bin edge, raster
+        kernel split and raster CTAs per SM for each MSAA class, and the bin capacity; kept in
+        the context and cached on disk."""
         indices = list(range(len(self.scenes))) if indices is None else list(indices)
         ptrs = [int(o) for o in outputs]
         arr = self._array(ptrs, indices)
-        best = (ctypes.c_int * 2)()
-        check(_lib.load().rast_autotune_batch(self._ctx, arr, len(indices), best), "autotune")
-        res = {"msaa1_tile": best[0], "msaa4_tile": best[1], "scenes": len(indices)}
+        t = _lib.Tuning()
+        check(_lib.load().rast_autotune_batch_ex(self._ctx, arr, len(indices), ctypes.byref(t)), "autotune")
+        res = {"msaa1_tile": t.tile[0], "msaa4_tile": t.tile[1],
+               "msaa1_heavy_entries": t.heavy_entries[0], "msaa4_heavy_entries": t.heavy_entries[1],
+               "msaa1_raster_ctas_per_sm": t.raster_ctas_per_sm[0], "msaa4_raster_ctas_per_sm": t.raster_ctas_per_sm[1],
+               "bin_capacity": t.bin_capacity, "batch_ms": t.batch_ms, "scenes": len(indices)}
         if cache:
             try:
                 os.makedirs(os.path.dirname(TUNE_CACHE), exist_ok=True)

@@ -36,6 +36,12 @@ void mat4_mul(const float* a, const float* b, float* out) {
     std::memcpy(out, r, sizeof(r));
 }
 
+uint32_t heavy_bits_of(uint32_t min_entries) {
+    // a power of two: bins with at least 2^bits entries are heavy; all ones: none is
+    if (min_entries == 0xFFFFFFFFu) return 32u;
+    return min_entries ? 31u - (uint32_t)__builtin_clz(min_entries) : 0u;
+}
+
 int choose_tile(int w, int h, int msaa, int req, uint64_t ntris) {
     if (req == 8 || req == 16 || req == 32) {
         long long n = (long long)((w + req - 1) / req) * ((h + req - 1) / req);
@@ -263,7 +269,8 @@ rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs) {
             a.raster_tile_offset = frames[i].tile_begin;
             a.raster_blocks = blocks;
             a.raster_queue = &E.d_state->queue[kQueueSlots * group];
-            a.raster_heavy_bits = E.heavy_bits;
+            a.raster_heavy_bits = E.heavy_bits[frames[i].msaa == 4 ? 1 : 0];
+            a.raster_ctas_per_sm = E.ctas_per_sm[frames[i].msaa == 4 ? 1 : 0];
             err = launch_raster(a, frames[i].msaa, frames[i].ts);
             i = j;
         }
@@ -383,9 +390,7 @@ rast_status rast_set_clear_depth(rast_ctx* c, float d) {
 
 rast_status rast_set_heavy_tile_entries(rast_ctx* c, uint32_t min_entries) {
     if (!c) return RAST_INVALID_ARG;
-    // a power of two: bins with at least 2^bits entries are heavy
-    c->E.heavy_bits = min_entries ? 31u - (uint32_t)__builtin_clz(min_entries) : 0u;
-    if (min_entries == 0xFFFFFFFFu) c->E.heavy_bits = 32u;
+    c->E.heavy_bits[0] = c->E.heavy_bits[1] = heavy_bits_of(min_entries);
     return RAST_OK;
 }
 
@@ -549,6 +554,8 @@ rast_status rast_stats(rast_ctx* c, uint64_t* shaded, uint64_t* fsinv, uint64_t*
 }
 
 void* rast_stream(rast_ctx* c) { return c ? (void*)c->E.stream : nullptr; }
+
+uint64_t rast_kernel_launches(void) { return kernel_launches(); }
 
 rast_status rast_set_profiling(rast_ctx* c, int enable) {
     if (!c) return RAST_INVALID_ARG;

@@ -1,5 +1,5 @@
 // rast_batch.cu - many independent scenes per launch sequence, CUDA-graph capture of a fixed
-// batch, and the tile-size autotuner.
+// batch, and the autotuner (bin edge, raster kernel split and CTA count, bin capacity).
 //
 // A batch is a list of frames handed to run_frames at once: the vertex, binning and scan
 // kernels run once over every scene, and the persistent raster kernel (one launch per
@@ -130,78 +130,139 @@ rast_status rast_render_batch(rast_ctx* c, const rast_scene* sc, uint32_t n) {
     return render_jobs(c, sc, n, jobs, host_off, staging);
 }
 
-rast_status rast_autotune_batch(rast_ctx* c, const rast_scene* sc, uint32_t n, int best_tiles[2]) {
+rast_status rast_autotune_batch_ex(rast_ctx* c, const rast_scene* sc, uint32_t n, rast_tuning* out) {
     if (!c || !sc || n == 0) return RAST_INVALID_ARG;
-    bool has1 = false, has4 = false;
-    for (uint32_t i = 0; i < n; ++i) (sc[i].msaa == 4 ? has4 : has1) = true;
-    const int sizes[3] = {8, 16, 32};
+    bool has[2] = {false, false};
+    for (uint32_t i = 0; i < n; ++i) has[sc[i].msaa == 4 ? 1 : 0] = true;
     std::vector<rast_scene> trial(sc, sc + n);
     // every trial writes into the staging buffer, not the caller's images
     size_t px = 0;
     for (uint32_t i = 0; i < n; ++i) px += (size_t)sc[i].width * sc[i].height;
     if (!c->batch_out.reserve(px)) return RAST_OOM;
-    float best_ms = 3.0e38f;
-    int best1 = 0, best4 = 0;
+    size_t off = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        trial[i].tile = 0;
+        trial[i].argb_out = c->batch_out.p + off;
+        off += (size_t)sc[i].width * sc[i].height;
+    }
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return RAST_CUDA_ERROR;
+    Engine& E = c->E;
+    const int saved_tile[2] = {c->tuned_tile[0], c->tuned_tile[1]};
+    const uint32_t saved_heavy[2] = {E.heavy_bits[0], E.heavy_bits[1]};
+    const int saved_ctas[2] = {E.ctas_per_sm[0], E.ctas_per_sm[1]};
     rast_status result = RAST_OK;
-    const int saved[2] = {c->tuned_tile[0], c->tuned_tile[1]};
-    for (int a = 0; a < (has1 ? 3 : 1) && result == RAST_OK; ++a)
-        for (int b = 0; b < (has4 ? 3 : 1) && result == RAST_OK; ++b) {
-            const int t1 = has1 ? sizes[a] : 0, t4 = has4 ? sizes[b] : 0;
-            size_t off = 0;
-            for (uint32_t i = 0; i < n; ++i) {
-                trial[i] = sc[i];
-                trial[i].tile = 0;
-                trial[i].argb_out = c->batch_out.p + off;
-                off += (size_t)sc[i].width * sc[i].height;
+    // mean batch time over two timed runs after one sizing run, with the current settings
+    auto time_batch = [&](float& ms) {
+        ms = 0.0f;
+        std::vector<FrameJob> jobs;
+        for (int rep = 0; rep < 3 && result == RAST_OK; ++rep) {
+            rast_status st = build_jobs(c, trial.data(), n, false, jobs, nullptr, nullptr);
+            if (st != RAST_OK) {
+                result = st;
+                return;
             }
-            c->tuned_tile[0] = t1;
-            c->tuned_tile[1] = t4;
-            std::vector<FrameJob> jobs;
+            E.sync_after = true;
+            cudaEventRecord(e0, E.stream);
+            st = run_frames(E, jobs);
+            cudaEventRecord(e1, E.stream);
+            cudaEventSynchronize(e1);
+            if (st != RAST_OK && st != RAST_TEXTURE_OOB) {
+                result = st;
+                return;
+            }
+            c->batch_hints.resize(n);
+            for (uint32_t i = 0; i < n; ++i)
+                c->batch_hints[i] = std::max<uint64_t>(c->batch_hints[i], jobs[i].need + jobs[i].need / 8);
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0) ms += t / 2.0f;  // the first run sizes buffers
+        }
+    };
+    // 1. bin edge per MSAA class (8, 16 or 32 pixels), both classes together
+    const int sizes[3] = {8, 16, 32};
+    float best_ms = 3.0e38f;
+    int best_tile[2] = {0, 0};
+    for (int a = 0; a < (has[0] ? 3 : 1) && result == RAST_OK; ++a)
+        for (int b = 0; b < (has[1] ? 3 : 1) && result == RAST_OK; ++b) {
+            c->tuned_tile[0] = has[0] ? sizes[a] : 0;
+            c->tuned_tile[1] = has[1] ? sizes[b] : 0;
             float ms = 0.0f;
-            for (int rep = 0; rep < 3 && result == RAST_OK; ++rep) {
-                rast_status st = build_jobs(c, trial.data(), n, false, jobs, nullptr, nullptr);
-                if (st != RAST_OK) {
-                    result = st;
-                    break;
-                }
-                c->E.sync_after = true;
-                cudaEventRecord(e0, c->E.stream);
-                st = run_frames(c->E, jobs);
-                cudaEventRecord(e1, c->E.stream);
-                cudaEventSynchronize(e1);
-                if (st != RAST_OK && st != RAST_TEXTURE_OOB) {
-                    result = st;
-                    break;
-                }
-                c->batch_hints.resize(n);
-                for (uint32_t i = 0; i < n; ++i)
-                    c->batch_hints[i] = std::max<uint64_t>(c->batch_hints[i], jobs[i].need + jobs[i].need / 8);
-                float t = 0.0f;
-                cudaEventElapsedTime(&t, e0, e1);
-                if (rep > 0) ms += t;  // the first run sizes buffers
-            }
+            time_batch(ms);
             if (result == RAST_OK && ms < best_ms) {
                 best_ms = ms;
-                best1 = t1;
-                best4 = t4;
+                best_tile[0] = c->tuned_tile[0];
+                best_tile[1] = c->tuned_tile[1];
             }
         }
+    c->tuned_tile[0] = best_tile[0];
+    c->tuned_tile[1] = best_tile[1];
+    // 2. per class: the split between the CTA-wide and the warp-per-tile raster kernel, and
+    // the persistent raster CTAs per SM
+    const uint32_t heavy_opts[3] = {0u, 9u, 32u};  // every bin CTA-wide, bins of 512+ entries, none
+    const int cta_opts[3] = {0, 4, 2};
+    for (int cls = 0; cls < 2 && result == RAST_OK; ++cls) {
+        if (!has[cls]) continue;
+        uint32_t bh = E.heavy_bits[cls];
+        int bc = E.ctas_per_sm[cls];
+        for (uint32_t h : heavy_opts)
+            for (int k : cta_opts) {
+                if (result != RAST_OK) break;
+                if (h == bh && k == bc) continue;  // the current setting was timed already
+                E.heavy_bits[cls] = h;
+                E.ctas_per_sm[cls] = k;
+                float ms = 0.0f;
+                time_batch(ms);
+                if (result == RAST_OK && ms < best_ms) {
+                    best_ms = ms;
+                    bh = h;
+                    bc = k;
+                }
+            }
+        E.heavy_bits[cls] = bh;
+        E.ctas_per_sm[cls] = bc;
+    }
+    // 3. bin capacity: one run with the chosen settings measures each scene's bins; the batch
+    // reserves that plus an eighth (batch_hints), instead of the first estimate
+    uint64_t cap = 0;
+    if (result == RAST_OK) {
+        c->batch_hints.assign(n, 0);
+        float ms = 0.0f;
+        time_batch(ms);
+        for (uint32_t i = 0; i < n && result == RAST_OK; ++i) cap += c->batch_hints[i];
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (result != RAST_OK) {
-        c->tuned_tile[0] = saved[0];
-        c->tuned_tile[1] = saved[1];
+        c->tuned_tile[0] = saved_tile[0];
+        c->tuned_tile[1] = saved_tile[1];
+        for (int k = 0; k < 2; ++k) {
+            E.heavy_bits[k] = saved_heavy[k];
+            E.ctas_per_sm[k] = saved_ctas[k];
+        }
         return result;
     }
-    c->tuned_tile[0] = best1;
-    c->tuned_tile[1] = best4;
-    if (best_tiles) {
-        best_tiles[0] = best1;
-        best_tiles[1] = best4;
+    if (out) {
+        for (int k = 0; k < 2; ++k) {
+            out->tile[k] = c->tuned_tile[k];
+            const uint32_t hb = E.heavy_bits[k];
+            out->heavy_entries[k] = hb == 0 ? 0u : hb >= 32 ? 0xFFFFFFFFu : 1u << hb;
+            out->raster_ctas_per_sm[k] = E.ctas_per_sm[k];
+        }
+        out->bin_capacity = cap;
+        out->batch_ms = best_ms;
     }
     return RAST_OK;
+}
+
+rast_status rast_autotune_batch(rast_ctx* c, const rast_scene* sc, uint32_t n, int best_tiles[2]) {
+    rast_tuning t;
+    const rast_status st = rast_autotune_batch_ex(c, sc, n, &t);
+    if (st == RAST_OK && best_tiles) {
+        best_tiles[0] = t.tile[0];
+        best_tiles[1] = t.tile[1];
+    }
+    return st;
 }
 
 rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, rast_batch** out) {
@@ -211,6 +272,11 @@ rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, ras
     b->ctx = c;
     rast_status st = build_jobs(c, sc, n, false, b->jobs, nullptr, nullptr);
     if (st == RAST_OK && !b->E.init()) st = RAST_CUDA_ERROR;
+    // the context's (autotuned) raster settings
+    for (int k = 0; k < 2; ++k) {
+        b->E.heavy_bits[k] = c->E.heavy_bits[k];
+        b->E.ctas_per_sm[k] = c->E.ctas_per_sm[k];
+    }
     if (st == RAST_OK) {
         // one synchronous run sizes every buffer of this batch's own engine
         b->E.sync_after = true;

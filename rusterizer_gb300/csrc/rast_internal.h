@@ -195,7 +195,11 @@ struct Engine {
     DeviceState* d_state = nullptr;
     DeviceState* h_state = nullptr;
     uint64_t clip_hint = 0;
-    uint32_t heavy_bits = kDefaultHeavyBits;  // bins of >= 2^heavy_bits entries: CTA-wide raster
+    // raster settings per MSAA class ([0] MSAA 1, [1] MSAA 4): bins of >= 2^heavy_bits entries
+    // are rastered CTA-wide, the others one warp per tile; persistent raster CTAs per SM (0: as
+    // many as fit)
+    uint32_t heavy_bits[2] = {kDefaultHeavyBits, kDefaultHeavyBits};
+    int ctas_per_sm[2] = {0, 0};
     bool sync_after = true;
     bool profiling = false;
     cudaEvent_t ev[6] = {};
@@ -251,6 +255,8 @@ void mat4_mul(const float* a, const float* b, float* out);
 // 0 when no bin size fits.
 constexpr uint64_t kAutoBigBinTris = 8192;
 int choose_tile(int w, int h, int msaa, int req, uint64_t ntris);
+// rast_set_heavy_tile_entries' threshold as a bit length (32: no bin is heavy)
+uint32_t heavy_bits_of(uint32_t min_entries);
 rast_status run_frames(Engine& E, std::vector<FrameJob>& jobs);
 
 }  // namespace rast

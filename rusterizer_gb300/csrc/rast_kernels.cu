@@ -1650,9 +1650,14 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
 
 // Launch with programmatic stream serialization (see pdl_enter): the kernel may be scheduled
 // while its predecessor in the stream is still running and waits for it on entry.
+// Pipeline kernels launched by this process (counted at enqueue, or at capture for graphs).
+static std::atomic<unsigned long long> g_launches{0};
+unsigned long long kernel_launches() { return g_launches.load(std::memory_order_relaxed); }
+
 template <typename... KArgs, typename... Args>
 static cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
                               cudaStream_t stream, Args... args) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
@@ -1723,6 +1728,11 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
     if (e != cudaSuccess) return e;
     e = persistent_grid(k_raster_warp<S, TS>, 32 * kWarpUnitWarps, wbytes, warp_cap, wgrid_cap);
     if (e != cudaSuccess) return e;
+    if (a.raster_ctas_per_sm > 0) {
+        const int cap = a.raster_ctas_per_sm * sm_count();
+        grid_cap = grid_cap < cap ? grid_cap : cap;
+        wgrid_cap = wgrid_cap < cap ? wgrid_cap : cap;
+    }
     if (a.raster_blocks == 0) return cudaSuccess;
     e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
                    a.scratch.tile_order, a.raster_queue, a.scratch.status, a.raster_heavy_bits);

@@ -27,6 +27,7 @@ struct LaunchArgs {
     uint32_t raster_blocks;        // tiles in the group
     unsigned int* raster_queue;    // the group's kQueueSlots tile-queue counters (zeroed per frame)
     uint32_t raster_heavy_bits;    // bins of >= 2^bits entries are rastered CTA-wide (32: none)
+    int raster_ctas_per_sm;        // persistent raster CTAs per SM (0: as many as fit)
     Scratch scratch;
 };
 
@@ -36,6 +37,7 @@ cudaError_t launch_scans(const LaunchArgs& a);
 cudaError_t launch_bin_scatter(const LaunchArgs& a);
 cudaError_t launch_raster(const LaunchArgs& a, int msaa, int ts);
 size_t raster_smem(int msaa, int ts);
+unsigned long long kernel_launches();
 
 }  // namespace rast
 

@@ -285,6 +285,11 @@ rast_status rast_server_create(rast_ctx* c, const rast_server_config* cfg, rast_
     s->nslots = (s->cfg.streams == 2 && !s->cfg.one_per_launch) ? 2 : 1;
     for (int i = 0; i < s->nslots; ++i) {
         s->slots[i].server = s;
+        // the context's (autotuned) raster settings
+        for (int k = 0; k < 2; ++k) {
+            s->slots[i].E.heavy_bits[k] = c->E.heavy_bits[k];
+            s->slots[i].E.ctas_per_sm[k] = c->E.ctas_per_sm[k];
+        }
         if (!s->slots[i].E.init()) {
             delete s;
             return RAST_CUDA_ERROR;
