@@ -36,16 +36,17 @@ AUTO_BIG_BIN_TRIS = 8192  # from this many triangles the library picks 32-pixel 
 
 
 def launches_per_frame(width, height, ntris, tile=0):
-    """Kernels per plain frame: vertex, bin count, clip, column scan, tile scan, scatter, tile
-    order, raster, plus the quadrant split when the frame uses 32-pixel bins (the library's
-    automatic choice: 32-pixel bins for frames of AUTO_BIG_BIN_TRIS triangles or more, else 16,
-    either one when the other would exceed MAX_TILES_PER_FRAME bins)."""
+    """Kernels per plain frame: vertex, bin count, clip, column scan, tile scan (which also
+    builds the raster tile queue of a one-frame run), scatter, raster, plus the quadrant split
+    when the frame uses 32-pixel bins (the library's automatic choice: 32-pixel bins for frames
+    of AUTO_BIG_BIN_TRIS triangles or more, else 16, either one when the other would exceed
+    MAX_TILES_PER_FRAME bins)."""
     def fits(t):
         return -(-width // t) * -(-height // t) <= MAX_TILES_PER_FRAME
     if not (tile in (8, 16, 32) and fits(tile)):
         order = (32, 16) if ntris >= AUTO_BIG_BIN_TRIS else (16, 32)
         tile = next(t for t in order if fits(t))
-    return 9 if tile == 32 else 8
+    return 8 if tile == 32 else 7
 
 
 def batch_tile(scene, tuned):
@@ -55,7 +56,7 @@ def batch_tile(scene, tuned):
     if t in (8, 16, 32):
         return t
     from rusterizer_gb300 import scenes
-    return 32 if launches_per_frame(scene["width"], scene["height"], scenes.scene_triangles(scene)) == 9 else 16
+    return 32 if launches_per_frame(scene["width"], scene["height"], scenes.scene_triangles(scene)) == 8 else 16
 
 
 L2_NOTE = "GPU arm: L2 flushed (256 MB write) before every timed frame"
@@ -504,7 +505,37 @@ def run_ours(args):
             for _ in range(n):
                 self.step()
 
+    class PipelinedLane(E2ELane):
+        """One host thread, two resident meshes used in turn: each step streams the next step's
+        mesh with rast_mesh_update_async (its copies overlap the current frame) and renders the
+        current mesh into pinned host memory with rast_framebuffer."""
+
+        def __init__(self):
+            super().__init__()
+            self.m2 = renderer.Mesh(d0["pos"], d0["uv"], d0["idx"])
+            self.handles = [self.mh, self.r.upload(self.m2)]
+            self.meshes = [self.m, self.m2]
+            self.k = 0
+
+        def step(self):
+            nxt = self.handles[(self.k + 1) % 2]
+            s = L.rast_mesh_update_async(self.r._ctx, nxt, ctypes.cast(self.npos.data_ptr(), fp),
+                                         ctypes.cast(self.nuv.data_ptr(), fp), None,
+                                         ctypes.cast(self.nidx.data_ptr(), u32p))
+            assert s == 0, s
+            self.r.render(self.meshes[self.k % 2], renderer.VS_MVP, d0.get("fs", 0))
+            s = L.rast_framebuffer(self.r._ctx, ctypes.c_void_p(self.out.data_ptr()))
+            assert s == 0, s
+            self.k += 1
+
     lanes = [E2ELane() for _ in range(2)]
+    piped = PipelinedLane()
+    piped.run(max(args.warmup, 3))
+    barrier()
+    t0 = time.perf_counter()
+    piped.run(args.steps)
+    barrier()
+    piped_s = time.perf_counter() - t0
     for ln in lanes:
         ln.run(max(args.warmup, 3))
     # one lane alone (every call back to back) ...
@@ -525,15 +556,16 @@ def run_ours(args):
         th.join()
     barrier()
     e2e_s = time.perf_counter() - t0
-    e2e_s, serial_s = reps.max([e2e_s, serial_s])
+    e2e_s, serial_s, piped_s = reps.max([e2e_s, serial_s, piped_s])
     e2e_value = world * args.steps / e2e_s
     e2e_serial = world * args.steps / serial_s
+    e2e_piped = world * args.steps / piped_s
     queue()
     ref_img = r.framebuffer()
-    for ln in lanes:
+    for ln in lanes + [piped]:
         assert (ln.out.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
     h2d = lanes[0].npos.numel() * 4 + lanes[0].nuv.numel() * 4 + lanes[0].nidx.numel() * 4
-    for ln in lanes:
+    for ln in lanes + [piped]:
         ln.r.close()
 
     line = None
@@ -564,7 +596,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": W * H * 4, "host_threads": 2,
-                    "one_thread_value": e2e_serial},
+                    "one_thread_value": e2e_serial, "one_thread_pipelined_value": e2e_piped},
             "gpu_launches": timed_launches,
             "clocks": clk.summary(),
         }
@@ -595,7 +627,12 @@ def run_batched(args):
     dev = [torch.empty(s["height"] * s["width"], dtype=torch.int32, device="cuda") for s in sc]
     ptrs = [d.data_ptr() for d in dev]
     tuned = br.autotune(ptrs)
+    from rusterizer_gb300 import _lib as lib
+    n_launch0 = lib.load().rast_kernel_launches()
     g = br.capture(ptrs)
+    # rast_batch_create runs the batch once to size it, then captures the same launch sequence:
+    # half of its launches are the kernels of one replay
+    launches_per_replay = int(lib.load().rast_kernel_launches() - n_launch0) // 2
     ext = torch.cuda.ExternalStream(BatchRenderer.graph_stream(g))
     for _ in range(args.warmup):
         BatchRenderer.replay(g)
@@ -677,10 +714,7 @@ def run_batched(args):
             "cpu_baseline": cpu,
             "e2e": {"value": world * len(sc) / e2e_s, "unit": "scenes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(4 * s["width"] * s["height"] for s in sc))},
-            # per replay: vertex, bin count, clip, two scans, scatter, then for each (MSAA, bin
-            # size) group of the batch: tile order, quadrant split (32-pixel bins) and raster
-            "gpu_launches": args.steps * (6 + sum(3 if t == 32 else 2 for _, t in {
-                (s.get("msaa", 4), batch_tile(s, tuned)) for s in sc})),
+            "gpu_launches": args.steps * launches_per_replay,
             "clocks": clk.summary(),
         }), flush=True)
     br.close()

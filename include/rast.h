@@ -83,6 +83,15 @@ rast_status rast_mesh_free(rast_ctx* ctx, rast_mesh mesh);
  * next rast_framebuffer returns RAST_INVALID_ARG. */
 rast_status rast_mesh_update(rast_ctx* ctx, rast_mesh mesh, const float* pos, const float* uv,
                              const float* rgba, const uint32_t* idx);
+/* The same copies, enqueued without waiting (no counterpart in the reference): they start
+ * once the frames already enqueued on the context have finished, and the next rast_framebuffer
+ * or rast_framebuffer_async that draws this mesh waits for them on the device. The host arrays
+ * must stay unchanged until that frame has returned (rast_framebuffer) or its stream has been
+ * synchronised; page-locked arrays make the copies truly asynchronous. With two meshes used
+ * in turn, one host thread streams the next frame's mesh while the current frame renders.
+ * Synchronous updates, frees, batches and servers first wait for pending copies. */
+rast_status rast_mesh_update_async(rast_ctx* ctx, rast_mesh mesh, const float* pos, const float* uv,
+                                   const float* rgba, const uint32_t* idx);
 
 /* Uniforms::bind_texture (src/uniform.rs:29-33): slot must equal the number already bound.
  * rgba8 is w*h*4 bytes, row-major, (0,0) top-left (Texture, src/texture.rs:6-13). */

@@ -37,6 +37,7 @@ SIGNATURES = {
     "rast_mesh_upload": (_i, [_vp, _fp, _fp, _fp, _u32, _u32p, _u32, _u32p]),
     "rast_mesh_free": (_i, [_vp, _u32]),
     "rast_mesh_update": (_i, [_vp, _u32, _fp, _fp, _fp, _u32p]),
+    "rast_mesh_update_async": (_i, [_vp, _u32, _fp, _fp, _fp, _u32p]),
     "rast_texture_upload": (_i, [_vp, _i, _u8p, _i, _i]),
     "rast_set_uniforms": (_i, [_vp, _fp, _fp, _fp]),
     "rast_draw": (_i, [_vp, _u32, _i, _i]),

@@ -122,6 +122,7 @@ extern "C" {
 rast_status rast_render_batch(rast_ctx* c, const rast_scene* sc, uint32_t n) {
     if (!c || (n && !sc)) return RAST_INVALID_ARG;
     if (n == 0) return RAST_OK;
+    c->sync_copies();
     std::vector<FrameJob> jobs;
     std::vector<size_t> host_off;
     size_t staging = 0;
@@ -270,6 +271,7 @@ rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, ras
     rast_batch* b = new (std::nothrow) rast_batch();
     if (!b) return RAST_OOM;
     b->ctx = c;
+    c->sync_copies();
     rast_status st = build_jobs(c, sc, n, false, b->jobs, nullptr, nullptr);
     if (st == RAST_OK && !b->E.init()) st = RAST_CUDA_ERROR;
     // the context's (autotuned) raster settings

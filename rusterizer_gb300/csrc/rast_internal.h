@@ -80,6 +80,8 @@ struct MeshRec {
     uint32_t* idx = nullptr;
     uint32_t nverts = 0, ntris = 0;
     bool live = false;
+    cudaEvent_t ready = nullptr;  // end of the last rast_mesh_update_async copy
+    bool pending = false;         // that copy has not been waited for by a frame yet
     size_t bytes() const {
         return (size_t)nverts * (12 + 8 + (rgba ? 16 : 0)) + (size_t)ntris * 12;
     }
@@ -115,8 +117,11 @@ struct MeshRec {
         if (uv) cudaFree(uv);
         if (rgba) cudaFree(rgba);
         if (idx) cudaFree(idx);
+        if (ready) cudaEventDestroy(ready);
         pos = uv = rgba = nullptr;
         idx = nullptr;
+        ready = nullptr;
+        pending = false;
         live = false;
     }
 };
@@ -280,4 +285,15 @@ struct rast_ctx {
     int tuned_tile[2] = {0, 0};             // batch autotuner: MSAA 1, MSAA 4
     std::vector<uint64_t> batch_hints;      // bins needed per scene by the last batch
     rast::DevBuf<uint32_t> batch_out;       // staging for host-pointer batch outputs
+    // asynchronous mesh updates: their copies run on `copy` after the frames enqueued before
+    // them (`frame_done`, recorded after every frame), and frames wait for the mesh's `ready`
+    cudaStream_t copy = nullptr;
+    cudaEvent_t frame_done = nullptr;
+    bool frame_recorded = false;
+    // waits for every asynchronous mesh copy (before synchronous updates, frees and the batch
+    // and server paths, which do not track them)
+    void sync_copies() {
+        if (copy) cudaStreamSynchronize(copy);
+        for (rast::MeshRec& m : meshes) m.pending = false;
+    }
 };

@@ -432,11 +432,20 @@ __global__ void __launch_bounds__(1024) k_scan_cols(const FrameDev* __restrict__
     }
 }
 
-// One block (1024 threads) per frame: tile_start = exclusive prefix of tile_count.
+__device__ void tile_order_block(uint32_t tile0, uint32_t n, const uint32_t* __restrict__ tile_count,
+                                 uint32_t* __restrict__ order, unsigned int* __restrict__ queue, bool overflow,
+                                 uint32_t heavy_bits, uint32_t* cnt, uint32_t* off);
+
+// One block (1024 threads) per frame: tile_start = exclusive prefix of tile_count, capacity
+// check. For a run of one frame (order_queue set) the block also builds the raster tile queue
+// (tile_order_block), which saves the separate k_tile_order launch.
 __global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict__ frames,
-                                                     Scratch s) {
+                                                     Scratch s, uint32_t* __restrict__ order,
+                                                     unsigned int* __restrict__ order_queue,
+                                                     uint32_t heavy_bits) {
     pdl_enter();
     __shared__ uint32_t tmp[33];
+    __shared__ uint32_t cnt[33], off[33];
     const FrameDev& f = frames[blockIdx.x];
     const uint32_t nt = f.ntiles;
     const uint32_t per = (nt + blockDim.x - 1) / blockDim.x;
@@ -453,6 +462,11 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const FrameDev* __restrict_
     if (threadIdx.x == 0) {
         s.frame_need[blockIdx.x] = total;
         if ((unsigned long long)total > f.bin_cap) atomicOr(s.status, ST_BIN_OVERFLOW);
+    }
+    if (order_queue) {
+        __syncthreads();  // every tile_count read above is done before the queue is built
+        tile_order_block(f.tile_begin, nt, s.tile_count, order, order_queue,
+                         (unsigned long long)total > f.bin_cap, heavy_bits, cnt, off);
     }
 }
 
@@ -1598,22 +1612,16 @@ __global__ void __launch_bounds__(256) k_bin_split(const FrameDev* __restrict__ 
     }
 }
 
-// Tile queue of one raster launch: tiles with entries first, in decreasing order of entry
-// count (bucketed by bit length), then tiles without entries; queue[2] = tiles with entries,
-// queue[3] = the leading tiles with at least 2^heavy_bits entries (rastered CTA-wide by
-// k_raster; the rest one warp per tile by k_raster_warp). One block.
-__global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
-                                                     const uint32_t* __restrict__ tile_count,
-                                                     uint32_t* __restrict__ order,
-                                                     unsigned int* __restrict__ queue,
-                                                     const uint32_t* __restrict__ status,
-                                                     uint32_t heavy_bits) {
-    pdl_enter();
-    __shared__ uint32_t cnt[33], off[33];
+// Tile queue of one raster launch (block-wide, 1024 threads): tiles with entries first, in
+// decreasing order of entry count (bucketed by bit length), then tiles without entries;
+// queue[2] = tiles with entries, queue[3] = the leading tiles with at least 2^heavy_bits entries
+// (rastered CTA-wide by k_raster; the rest one warp per tile by k_raster_warp). After a bin
+// overflow every tile counts as empty (each is cleared and the host re-runs the frame).
+__device__ void tile_order_block(uint32_t tile0, uint32_t n, const uint32_t* __restrict__ tile_count,
+                                 uint32_t* __restrict__ order, unsigned int* __restrict__ queue, bool overflow,
+                                 uint32_t heavy_bits, uint32_t* cnt, uint32_t* off) {
     if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
     __syncthreads();
-    // after a bin overflow every tile is cleared and the host re-runs the frame
-    const bool overflow = (*(volatile const uint32_t*)status & ST_BIN_OVERFLOW) != 0;
     // lanes with the same bucket add once per warp (thousands of tiles share a few buckets)
     for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
         const uint32_t i = i0 + threadIdx.x;
@@ -1644,6 +1652,19 @@ __global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
         base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (b < 33u) order[tile0 + base + __popc(peers & lanemask_lt())] = tile0 + i;
     }
+}
+
+// The tile queue of one raster launch over a group of frames (tile_order_block). One block.
+__global__ void __launch_bounds__(1024) k_tile_order(uint32_t tile0, uint32_t n,
+                                                     const uint32_t* __restrict__ tile_count,
+                                                     uint32_t* __restrict__ order,
+                                                     unsigned int* __restrict__ queue,
+                                                     const uint32_t* __restrict__ status,
+                                                     uint32_t heavy_bits) {
+    pdl_enter();
+    __shared__ uint32_t cnt[33], off[33];
+    const bool overflow = (*(volatile const uint32_t*)status & ST_BIN_OVERFLOW) != 0;
+    tile_order_block(tile0, n, tile_count, order, queue, overflow, heavy_bits, cnt, off);
 }
 
 // ===================================================================== launchers
@@ -1734,9 +1755,12 @@ static cudaError_t launch_raster_t(const LaunchArgs& a, uint32_t nsx) {
         wgrid_cap = wgrid_cap < cap ? wgrid_cap : cap;
     }
     if (a.raster_blocks == 0) return cudaSuccess;
-    e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks, a.scratch.tile_count,
-                   a.scratch.tile_order, a.raster_queue, a.scratch.status, a.raster_heavy_bits);
-    if (e != cudaSuccess) return e;
+    if (!a.scan_order_queue) {  // else k_scan_tiles built the queue
+        e = launch_pdl(k_tile_order, 1, 1024, 0, a.stream, a.raster_tile_offset, a.raster_blocks,
+                       a.scratch.tile_count, a.scratch.tile_order, a.raster_queue, a.scratch.status,
+                       a.raster_heavy_bits);
+        if (e != cudaSuccess) return e;
+    }
     if (nsx > 1) {
         const unsigned sgrid = a.raster_blocks < (uint32_t)grid_cap ? a.raster_blocks : (unsigned)grid_cap;
         e = launch_pdl(k_bin_split, sgrid, 256, 0, a.stream, a.raster_frames, a.raster_nframes,
@@ -1800,7 +1824,9 @@ cudaError_t launch_scans(const LaunchArgs& a) {
         cudaError_t e = launch_pdl(k_scan_cols, a.scan_groups, 1024, 0, a.stream, a.frames, a.nframes, a.scratch);
         if (e != cudaSuccess) return e;
     }
-    if (a.nframes) return launch_pdl(k_scan_tiles, (unsigned)a.nframes, 1024, 0, a.stream, a.frames, a.scratch);
+    if (a.nframes)
+        return launch_pdl(k_scan_tiles, (unsigned)a.nframes, 1024, 0, a.stream, a.frames, a.scratch,
+                          a.scratch.tile_order, a.scan_order_queue, a.scan_heavy_bits);
     return cudaSuccess;
 }
 

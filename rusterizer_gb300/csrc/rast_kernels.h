@@ -20,6 +20,10 @@ struct LaunchArgs {
     uint32_t vertex_blocks;
     uint32_t scan_groups;  // 32-tile groups over all frames
     uint32_t max_tiles;    // largest per-frame tile count
+    // a run of one frame: k_scan_tiles builds the raster tile queue into these counters (with
+    // this heavy-tile threshold) and the raster launch skips k_tile_order; null otherwise
+    unsigned int* scan_order_queue;
+    uint32_t scan_heavy_bits;
     // raster launch over one (msaa, tile) group of consecutive frames
     const FrameDev* raster_frames;
     int raster_nframes;

@@ -238,6 +238,8 @@ extern "C" rast_status rast_render_noalloc(int width, int height, int msaa, int 
         a.raster_blocks = F.ntiles;
         a.raster_queue = dstate->queue;
         a.raster_heavy_bits = kDefaultHeavyBits;
+        a.scan_order_queue = dstate->queue;
+        a.scan_heavy_bits = kDefaultHeavyBits;
         Scratch& S = a.scratch;
         S.vclip = reinterpret_cast<float4*>(base + L.vclip);
         S.vscr = reinterpret_cast<float4*>(base + L.vscr);

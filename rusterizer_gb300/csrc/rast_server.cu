@@ -280,6 +280,7 @@ rast_status rast_server_create(rast_ctx* c, const rast_server_config* cfg, rast_
     rast_server* s = new (std::nothrow) rast_server();
     if (!s) return RAST_OOM;
     s->ctx = c;
+    c->sync_copies();
     if (cfg) s->cfg = *cfg;
     if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = 40ull << 30;
     s->nslots = (s->cfg.streams == 2 && !s->cfg.one_per_launch) ? 2 : 1;
