@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "librast.so")
 SOURCES = ["rast_kernels.cu", "rast_api.cu", "rast_noalloc.cu", "rast_batch.cu", "rast_server.cu"]
-HEADERS = ["rast_device.cuh", "rast_types.h", "rast_kernels.h", "rast_internal.h"]
+HEADERS = ["rast_device.cuh", "rast_raster_warp.cuh", "rast_types.h", "rast_kernels.h", "rast_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true",
                   "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",

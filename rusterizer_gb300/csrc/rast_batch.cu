@@ -200,7 +200,8 @@ rast_status rast_autotune_batch_ex(rast_ctx* c, const rast_scene* sc, uint32_t n
     c->tuned_tile[1] = best_tile[1];
     // 2. per class: the split between the CTA-wide and the warp-per-tile raster kernel, and
     // the persistent raster CTAs per SM
-    const uint32_t heavy_opts[3] = {0u, 9u, 32u};  // every bin CTA-wide, bins of 512+ entries, none
+    // every bin CTA-wide; bins of 128+, 512+ or 2048+ entries CTA-wide; every bin one warp each
+    const uint32_t heavy_opts[5] = {0u, 7u, 9u, 11u, 32u};
     const int cta_opts[3] = {0, 4, 2};
     for (int cls = 0; cls < 2 && result == RAST_OK; ++cls) {
         if (!has[cls]) continue;

@@ -425,8 +425,10 @@ __global__ void __launch_bounds__(1024) k_scan_cols(const FrameDev* __restrict__
         uint32_t run = part[seg][tl];
         for (uint32_t r = r0; r < r1; ++r) {
             uint32_t* p = &base[(unsigned long long)r * nt + t];
-            uint32_t c = *p;
-            *p = run;
+            const uint32_t c = *p;
+            // the scatter reads a chunk's offset only for bins the chunk has entries in: empty
+            // cells keep their 0 (most of the matrix for dense meshes) and are not written
+            if (c) *p = run;
             run += c;
         }
     }
@@ -812,11 +814,9 @@ __device__ __forceinline__ float edge_room(float nx, float ny, float Px, float P
 // computed in f32 to within 0.03 pixel whenever it falls near the tile (|pal - gk / nal| below
 // 2^16; farther out only its sign matters), and the interval is widened by 1/8 pixel.
 // Non-finite points are not trimmed.
-template <int S, int TS, typename SM>
-__device__ __forceinline__ void line_span(const SM& sm, uint32_t it, uint32_t mode, uint32_t lc,
-                                          uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
-    const float px[3] = {sm.ipx[0][it], sm.ipx[1][it], sm.ipx[2][it]};
-    const float py[3] = {sm.ipy[0][it], sm.ipy[1][it], sm.ipy[2][it]};
+template <int S, int TS>
+__device__ __forceinline__ void line_span_pts(const float px[3], const float py[3], uint32_t mode, uint32_t lc,
+                                              uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
     bool finite = true;
 #pragma unroll
     for (int k = 0; k < 3; ++k) finite = finite && isfinite(px[k]) && isfinite(py[k]);
@@ -848,6 +848,15 @@ __device__ __forceinline__ void line_span(const SM& sm, uint32_t it, uint32_t mo
     if (hi < lo) hi = lo;
     a0 = (uint32_t)lo;
     a1 = (uint32_t)hi;
+}
+
+// line_span of item `it` of a shared-memory item batch.
+template <int S, int TS, typename SM>
+__device__ __forceinline__ void line_span(const SM& sm, uint32_t it, uint32_t mode, uint32_t lc,
+                                          uint32_t X0, uint32_t Y0, uint32_t& a0, uint32_t& a1) {
+    const float px[3] = {sm.ipx[0][it], sm.ipx[1][it], sm.ipx[2][it]};
+    const float py[3] = {sm.ipy[0][it], sm.ipy[1][it], sm.ipy[2][it]};
+    line_span_pts<S, TS>(px, py, mode, lc, X0, Y0, a0, a1);
 }
 
 // Order-preserving map of floats to unsigned integers (NaN above +inf) and back.

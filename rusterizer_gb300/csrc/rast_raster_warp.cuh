@@ -1,11 +1,11 @@
 // rast_raster_warp.cuh - warp-per-tile raster for light tiles (included by rast_kernels.cu).
 //
-// A raster tile with few bin entries (the common case for dense meshes of subpixel triangles:
-// about 70 entries, 270 candidate pixels and 100 fragments per 16x16 tile at 4K) leaves the
-// eight warps of the CTA-wide kernel (k_raster) mostly idle or running partial warps between
-// block barriers. Here one warp owns a whole tile: it stages the tile's items 32 at a time
-// (one per lane), walks their candidate pixels 32 at a time, depth-tests the covered fragments
-// in submission order and shades the passed ones, with full warps and no block barrier. The
+// A raster tile with few bin entries leaves the warps of the CTA-wide kernel (k_raster) running
+// partial warps between block barriers. Here one warp owns a whole tile: it stages the tile's
+// items 32 at a time, one per lane and held in that lane's registers (other lanes read them
+// with shuffles, which keeps shared memory for the samples and rings: 5 CTAs of 4 warps per
+// SM), walks their candidate pixels 32 at a time, depth-tests the covered fragments in
+// submission order and shades the passed ones, with full warps and no block barrier. The
 // arithmetic is the same device functions as k_raster (coverage, sample depths, tie rule,
 // interpolation, shaders, resolve), so results are bit-identical; only the work split differs.
 //
@@ -14,18 +14,15 @@
 // without entries. k_raster takes the heavy tiles.
 
 constexpr int kWarpUnitWarps = 4;  // warps (independent tiles) per CTA of k_raster_warp
+constexpr int kWarpUnitCtas = 5;   // CTAs per SM the launch bounds aim at
 
 template <int S, int TS>
 struct alignas(16) WarpUnitSmem {
     static constexpr int NPIX = TS * TS;
-    static constexpr int IB = 32;  // items per batch (one per lane when staged)
+    static constexpr int IB = 32;  // items per batch (one per lane)
     static constexpr int QC = 64;  // ring entries
     float zb[NPIX * S];            // sample-major: sample k of pixel p at k * NPIX + p
     uint32_t cb[NPIX * S];
-    float ipx[3][IB], ipy[3][IB], iz[3][IB], iw[3][IB], iinv[IB];
-    float iuv[6][IB];
-    uint32_t irect[IB];            // tile-local box x0 | y0 << 8 | x1 << 16 | y1 << 24 (0: nothing)
-    uint32_t itri[IB], imeta[IB];
     uint8_t rpre[IB][TS];          // rows trimmed by line_span: candidates before each box row
                                    // (at most 15 rows of 16 before the last: fits a byte)
     uint8_t rsta[IB][TS];          // rows trimmed by line_span: first column of each box row
@@ -54,73 +51,81 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     return v;
 }
 
-// Stages the items of one bin entry (a triangle, or the fan of its clipped polygon) at
-// positions first.. of the warp's batch, as stage_entry does for k_raster.
-template <int S, int TS>
-__device__ __forceinline__ void wstage_entry(WarpUnitSmem<S, TS>& sm, const FrameDev& f,
-                                             const DrawDev* __restrict__ draws, const Scratch& s, uint32_t g,
-                                             uint32_t aux, uint32_t nitems, uint32_t first, uint32_t X0,
-                                             uint32_t Y0, float ztile) {
+// One item of a warp batch (a triangle, or one fan triangle of a clipped polygon), held by the
+// lane of its slot: screen points, depths, w, texture coordinates, 1 / 2x area, tile-local box
+// (x0 | y0 << 8 | x1 << 16 | y1 << 24, 0: nothing to do), frame triangle and draw << 8 | sub.
+struct WItem {
+    float px[3], py[3], z[3], w[3], inv;
+    float uv[6];
+    uint32_t rect, tri, meta;
+};
+
+// Stages item k of a bin entry (triangle g, clipped polygon at aux or kNone) into `it`, as
+// stage_entry does for k_raster.
+template <int TS>
+__device__ __forceinline__ void wstage_item(WItem& it, const FrameDev& f, const DrawDev* __restrict__ draws,
+                                            const Scratch& s, uint32_t g, uint32_t aux, uint32_t k, uint32_t X0,
+                                            uint32_t Y0, float ztile) {
     const uint32_t di = find_draw(draws, f, g);
     const DrawDev& d = draws[di];
-    const int fs = d.fs;
-    for (uint32_t k = 0; k < nitems; ++k) {
-        const uint32_t it = first + k;
-        float4 sv[3];
-        float uv[3][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-        if (aux == kNone) {
-            const uint32_t tri = g - d.tbase;
-            const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
-                                    __ldg(d.idx + 3ull * tri + 2)};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                sv[q] = s.vscr[d.vbase + ii[q]];
-                if (fs == 0) {
-                    uv[q][0] = __ldg(d.uv + 2ull * ii[q]);
-                    uv[q][1] = __ldg(d.uv + 2ull * ii[q] + 1);
-                }
-            }
-        } else {
-            const float* st = s.clip_store + aux + 1;
-            const uint32_t vi[3] = {0u, k + 1, k + 2};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float* o = st + 10 * vi[q];
-                sv[q] = make_float4(o[0], o[1], o[2], o[3]);
-                uv[q][0] = o[8];
-                uv[q][1] = o[9];
-            }
-        }
+    float4 sv[3];
+    float uv[3][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    if (aux == kNone) {
+        const uint32_t tri = g - d.tbase;
+        const uint32_t ii[3] = {__ldg(d.idx + 3ull * tri), __ldg(d.idx + 3ull * tri + 1),
+                                __ldg(d.idx + 3ull * tri + 2)};
+        const bool tex = d.fs == 0;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            sm.ipx[q][it] = sv[q].x;
-            sm.ipy[q][it] = sv[q].y;
-            sm.iz[q][it] = sv[q].z;
-            sm.iw[q][it] = sv[q].w;
-            sm.iuv[2 * q][it] = uv[q][0];
-            sm.iuv[2 * q + 1][it] = uv[q][1];
+            sv[q] = s.vscr[d.vbase + ii[q]];
+            if (tex) {
+                uv[q][0] = __ldg(d.uv + 2ull * ii[q]);
+                uv[q][1] = __ldg(d.uv + 2ull * ii[q] + 1);
+            }
         }
-        // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
-        sm.iinv[it] = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
-        uint32_t bx0, bx1, by0, by1;
-        pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
-        const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
-        const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
-        // hidden items (depth_cull) cover nothing that could pass the strict depth test
-        const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1 &&
-                              !depth_cull(sv[0].z, sv[1].z, sv[2].z, ztile);
-        sm.irect[it] = nonempty ? ((cx0 - X0) | ((cy0 - Y0) << 8) | ((cx1 - X0) << 16) | ((cy1 - Y0) << 24)) : 0u;
-        sm.itri[it] = g;
-        sm.imeta[it] = (di << 8) | k;
+    } else {
+        const float* st = s.clip_store + aux + 1;
+        const uint32_t vi[3] = {0u, k + 1, k + 2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float* o = st + 10 * vi[q];
+            sv[q] = make_float4(o[0], o[1], o[2], o[3]);
+            uv[q][0] = o[8];
+            uv[q][1] = o[9];
+        }
     }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        it.px[q] = sv[q].x;
+        it.py[q] = sv[q].y;
+        it.z[q] = sv[q].z;
+        it.w[q] = sv[q].w;
+        it.uv[2 * q] = uv[q][0];
+        it.uv[2 * q + 1] = uv[q][1];
+    }
+    // 1 / triangle_2x_area (RasterizerTriangle::new, src/rasterizer/mod.rs:206)
+    it.inv = 1.0f / tri2x_area(sv[0].x, sv[0].y, sv[1].x, sv[1].y, sv[2].x, sv[2].y);
+    uint32_t bx0, bx1, by0, by1;
+    pixel_bbox(sv, f.width, f.height, bx0, bx1, by0, by1);
+    const uint32_t cx0 = max(bx0, X0), cx1 = min(bx1, X0 + TS);
+    const uint32_t cy0 = max(by0, Y0), cy1 = min(by1, Y0 + TS);
+    // hidden items (depth_cull) cover nothing that could pass the strict depth test
+    const bool nonempty = bx0 < bx1 && by0 < by1 && cx0 < cx1 && cy0 < cy1 &&
+                          !depth_cull(sv[0].z, sv[1].z, sv[2].z, ztile);
+    it.rect = nonempty ? ((cx0 - X0) | ((cy0 - Y0) << 8) | ((cx1 - X0) << 16) | ((cy1 - Y0) << 24)) : 0u;
+    it.tri = g;
+    it.meta = (di << 8) | k;
 }
+
+__device__ __forceinline__ float shfl_f(float v, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, v, src); }
+__device__ __forceinline__ uint32_t shfl_u(uint32_t v, uint32_t src) { return __shfl_sync(0xFFFFFFFFu, v, src); }
 
 // Depth test of up to 32 queued fragments (lane = fragment, ring order = submission order):
 // fragments of one pixel in rounds of increasing rank, as warp_depth does for k_raster.
 template <int S, int TS>
-__device__ __forceinline__ void wdepth(WarpUnitSmem<S, TS>& sm, uint32_t head, uint32_t n, uint32_t& stail,
-                                       const Scratch& s, uint32_t X0, uint32_t Y0, uint32_t& shaded,
-                                       uint32_t& fsinv) {
+__device__ __forceinline__ void wdepth(WarpUnitSmem<S, TS>& sm, const WItem& my, uint32_t head, uint32_t n,
+                                       uint32_t& stail, const Scratch& s, uint32_t X0, uint32_t Y0,
+                                       uint32_t& shaded, uint32_t& fsinv) {
     using U = WarpUnitSmem<S, TS>;
     const uint32_t lane = lane_id();
     const bool valid = lane < n;
@@ -135,6 +140,12 @@ __device__ __forceinline__ void wdepth(WarpUnitSmem<S, TS>& sm, uint32_t head, u
         cov = sm.qcov[q];
 #pragma unroll
         for (int k = 0; k < S; ++k) z[k] = sm.qz[k][q];
+    }
+    // the fragment log (debug) names the fragment's triangle: read from the item's lane
+    uint32_t ltri = 0, lmeta = 0;
+    if (s.log) {
+        ltri = shfl_u(my.tri, it);
+        lmeta = shfl_u(my.meta, it);
     }
     const uint32_t key = valid ? pix : 0x10000u + lane;
     const uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
@@ -151,8 +162,7 @@ __device__ __forceinline__ void wdepth(WarpUnitSmem<S, TS>& sm, uint32_t head, u
             dm |= (uint32_t)pass << k;
         }
         if (s.log && act)
-            log_fragment(s, sm.itri[it], sm.imeta[it] & 0xFFu, ((Y0 + pix / TS) << 16) | (X0 + pix % TS),
-                         (dm << 8) | cov);
+            log_fragment(s, ltri, lmeta & 0xFFu, ((Y0 + pix / TS) << 16) | (X0 + pix % TS), (dm << 8) | cov);
         __syncwarp();
     }
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, dm != 0);
@@ -170,18 +180,29 @@ __device__ __forceinline__ void wdepth(WarpUnitSmem<S, TS>& sm, uint32_t head, u
 }
 
 // Fragment shader and colour write of up to 32 fragments of the shade ring, as warp_shade does
-// for k_raster (kept out of line for the instruction cache).
+// for k_raster; each lane reads its fragment's item from the item's lane.
 template <int S, int TS>
-__device__ __noinline__ void wshade(WarpUnitSmem<S, TS>& sm, const float* inv255, uint32_t head, uint32_t n,
-                                    const DrawDev* __restrict__ draws, const FrameDev& f, const Scratch& s,
-                                    uint32_t X0, uint32_t Y0, uint32_t& oobc) {
+__device__ __forceinline__ void wshade(WarpUnitSmem<S, TS>& sm, const WItem& my, const float* inv255,
+                                      uint32_t head, uint32_t n, const DrawDev* __restrict__ draws,
+                                      const FrameDev& f, const Scratch& s, uint32_t X0, uint32_t Y0,
+                                      uint32_t& oobc) {
     using U = WarpUnitSmem<S, TS>;
     const uint32_t lane = lane_id();
     const bool valid = lane < n;
     const uint32_t q = (head + lane) & (U::QC - 1);
+    const uint32_t it = valid ? sm.sitem[q] : 0u;
+    float px[3], py[3], w[3], tuv[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        px[k] = shfl_f(my.px[k], it);
+        py[k] = shfl_f(my.py[k], it);
+        w[k] = shfl_f(my.w[k], it);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) tuv[k] = shfl_f(my.uv[k], it);
+    const uint32_t meta = shfl_u(my.meta, it), tri = shfl_u(my.tri, it);
     uint32_t argb = 0, pix = 0, dm = 0;
     if (valid) {
-        const uint32_t it = sm.sitem[q];
         pix = sm.spix[q];
         dm = sm.sdm[q];
         const uint32_t x = X0 + pix % TS, y = Y0 + pix / TS;
@@ -190,25 +211,26 @@ __device__ __noinline__ void wshade(WarpUnitSmem<S, TS>& sm, const float* inv255
         float e[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            float nx, ny;
-            item_normal(sm, it, k, nx, ny);
-            e[k] = edge_eval(nx, ny, sm.ipx[k][it], sm.ipy[k][it], xs, ys);
+            // inward normal of edge k (RasterizerTriangle::new, src/rasterizer/mod.rs:199-204)
+            const int nk = k == 2 ? 0 : k + 1;
+            const float nx = -(py[nk] - py[k]), ny = px[nk] - px[k];
+            e[k] = edge_eval(nx, ny, px[k], py[k], xs, ys);
         }
         float u, v, ww;
-        persp_bary(e[0], e[1], e[2], sm.iw[0][it], sm.iw[1][it], sm.iw[2][it], u, v, ww);
-        const DrawDev& d = draws[sm.imeta[it] >> 8];
+        persp_bary(e[0], e[1], e[2], w[0], w[1], w[2], u, v, ww);
+        const DrawDev& d = draws[meta >> 8];
         float col[4];
         if (d.fs == 0) {
             // FS::Texture (upstream src/main.rs:214-216)
-            const float tu = sm.iuv[0][it] * u + sm.iuv[2][it] * v + sm.iuv[4][it] * ww;
-            const float tv = sm.iuv[1][it] * u + sm.iuv[3][it] * v + sm.iuv[5][it] * ww;
+            const float tu = tuv[0] * u + tuv[2] * v + tuv[4] * ww;
+            const float tv = tuv[1] * u + tuv[3] * v + tuv[5] * ww;
             bool oob = false;
             tex_sample(d.tex, d.tex_w, d.tex_h, tu, tv, inv255, col, oob);
             if (oob) ++oobc;
         } else if (d.fs == 1) {
             // FS::Color (upstream src/main.rs:217)
             float vc[3][4];
-            item_colours(d, f, s, sm.itri[it], sm.imeta[it] & 0xFFu, vc);
+            item_colours(d, f, s, tri, meta & 0xFFu, vc);
 #pragma unroll
             for (int c = 0; c < 4; ++c) col[c] = vc[0][c] * u + vc[1][c] * v + vc[2][c] * ww;
         } else {
@@ -283,12 +305,13 @@ __device__ __forceinline__ void wresolve(const WarpUnitSmem<S, TS>& sm, const Fr
 }
 
 // One light tile by one warp: the bin's entries in submission order, 32 items at a time.
-// (A) each lane stages the items of one entry; (B) per item (lane) its candidate pixels: the
-// whole tile-local box, or for boxes of kTrimMin+ columns each row trimmed by line_span;
-// (C) the candidates 32 at a time - coverage (EdgeFunctions::eval, mod.rs:134-146) and sample
-// depths (RasterizerTriangle::fragment, mod.rs:225-253) - into the fragment ring, ordered depth
-// test into the shade ring, shading; both rings are drained before the next batch replaces the
-// items they refer to. Then the resolve.
+// (A) the items of the next entries, one per lane (a lane finds its entry and fan triangle
+// from the entries' running item counts); (B) per item (lane) its candidate pixels: the whole
+// tile-local box, or for boxes of kTrimMin+ columns each row trimmed by line_span; (C) the
+// candidates 32 at a time - coverage (EdgeFunctions::eval, mod.rs:134-146) and sample depths
+// (RasterizerTriangle::fragment, mod.rs:225-253) - into the fragment ring, ordered depth test
+// into the shade ring, shading; both rings are drained before the next batch replaces the items
+// they refer to. Then the resolve.
 template <int S, int TS>
 __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* inv255, const FrameDev& f,
                                           const DrawDev* __restrict__ draws, const Scratch& s,
@@ -308,6 +331,7 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
         }
     }
     __syncwarp();
+    WItem my;  // the item of this lane's slot in the current batch
     uint32_t pos = 0, batch = 0;
     // depth_cull bound: the clear depth at first; NaN (no culling) while the fragment log
     // records depth-failed fragments too
@@ -322,6 +346,7 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
         ++batch;
         // ---- A. items of the next entries that touch this tile, while they fit the batch
         uint32_t nit = 0;
+        my.rect = 0;
         while (pos < nent) {
             const uint32_t e = pos + lane;
             uint32_t g = 0, aux = kNone, nitems = 0;
@@ -342,23 +367,34 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
             // running item counts only grow along the lanes, so the entries that fit are a prefix
             const bool fits = e < nent && nit + incl <= (uint32_t)U::IB;
             const uint32_t take = __popc(__ballot_sync(0xFFFFFFFFu, fits));
-            if (fits && nitems) wstage_entry<S, TS>(sm, f, draws, s, g, aux, nitems, nit + incl - nitems, X0, Y0, zt);
-            if (take) nit += __shfl_sync(0xFFFFFFFFu, incl, take - 1);
+            const uint32_t win = take ? __shfl_sync(0xFFFFFFFFu, incl, take - 1) : 0u;  // items taken
+            // slot lane gets item q = lane - nit of this window: entry src, fan triangle k
+            const uint32_t qi = lane - nit;  // wraps for lanes below nit (not staged)
+            uint32_t src = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, src + st - 1);
+                if (v <= qi) src += st;
+            }
+            src = min(src, 31u);
+            const uint32_t sg = __shfl_sync(0xFFFFFFFFu, g, src), saux = __shfl_sync(0xFFFFFFFFu, aux, src);
+            const uint32_t sk = qi - (__shfl_sync(0xFFFFFFFFu, incl, src) - __shfl_sync(0xFFFFFFFFu, nitems, src));
+            if (lane >= nit && lane < nit + win) wstage_item<TS>(my, f, draws, s, sg, saux, sk, X0, Y0, zt);
+            nit += win;
             pos += take;
             if (take < 32) break;  // the batch is full, or the entries ran out
         }
-        __syncwarp();
         // ---- B. candidates of each item (lane = item)
         uint32_t c = 0, geo = 0;  // geo: x0 | y0 << 5 | w << 10 | h << 16 | trimmed << 21
         if (lane < nit) {
-            const uint32_t r = sm.irect[lane];
+            const uint32_t r = my.rect;
             const uint32_t x0 = r & 0xFFu, y0 = (r >> 8) & 0xFFu, x1 = (r >> 16) & 0xFFu, y1 = r >> 24;
             const uint32_t w = x1 - x0, h = y1 - y0;
             if (w >= kTrimMin && h > 0) {
                 uint32_t run = 0;
                 for (uint32_t row = 0; row < h; ++row) {
                     uint32_t a0 = x0, a1 = x1;
-                    line_span<S, TS>(sm, lane, 0u, y0 + row, X0, Y0, a0, a1);
+                    line_span_pts<S, TS>(my.px, my.py, 0u, y0 + row, X0, Y0, a0, a1);
                     sm.rsta[lane][row] = (uint8_t)a0;
                     sm.rpre[lane][row] = (uint8_t)run;
                     run += a1 - a0;
@@ -386,6 +422,12 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
             const uint32_t it = min(j, 31u);
             const uint32_t exc = __shfl_sync(0xFFFFFFFFu, incl - c, it);
             const uint32_t gg = __shfl_sync(0xFFFFFFFFu, geo, it);
+            // the item's points, depths and 1 / 2x area from its lane
+            const float p0x = shfl_f(my.px[0], it), p0y = shfl_f(my.py[0], it);
+            const float p1x = shfl_f(my.px[1], it), p1y = shfl_f(my.py[1], it);
+            const float p2x = shfl_f(my.px[2], it), p2y = shfl_f(my.py[2], it);
+            const float z0 = shfl_f(my.z[0], it), z1 = shfl_f(my.z[1], it), z2 = shfl_f(my.z[2], it);
+            const float inv = shfl_f(my.inv, it);
             uint32_t cov = 0, pix = 0;
             float z[S];
 #pragma unroll
@@ -409,17 +451,12 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
                 const uint32_t ly = y0 + row;
                 pix = ly * TS + col;
                 const float fx = (float)(X0 + col), fy = (float)(Y0 + ly);
-                float n0x, n0y, n1x, n1y, n2x, n2y;
-                item_normal(sm, it, 0, n0x, n0y);
-                item_normal(sm, it, 1, n1x, n1y);
-                item_normal(sm, it, 2, n2x, n2y);
-                const float p0x = sm.ipx[0][it], p0y = sm.ipy[0][it];
-                const float p1x = sm.ipx[1][it], p1y = sm.ipy[1][it];
-                const float p2x = sm.ipx[2][it], p2y = sm.ipy[2][it];
+                // inward normals (RasterizerTriangle::new, src/rasterizer/mod.rs:199-204)
+                const float n0x = -(p1y - p0y), n0y = p1x - p0x;
+                const float n1x = -(p2y - p1y), n1y = p2x - p1x;
+                const float n2x = -(p0y - p2y), n2y = p0x - p2x;
                 // tie rule per edge (EdgeFunctions::inside, mod.rs:148-170)
                 const bool t0 = edge_tie(n0x, n0y), t1 = edge_tie(n1x, n1y), t2 = edge_tie(n2x, n2y);
-                const float inv = sm.iinv[it];
-                const float z0 = sm.iz[0][it], z1 = sm.iz[1][it], z2 = sm.iz[2][it];
 #pragma unroll
                 for (int k = 0; k < S; ++k) {
                     const float xs = fx + sample_dx<S>(k), ys = fy + sample_dy<S>(k);
@@ -444,18 +481,18 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
             tail += __popc(bal);
             __syncwarp();
             if (tail - head >= 32) {
-                wdepth<S, TS>(sm, head, 32, stail, s, X0, Y0, shaded, fsinv);
+                wdepth<S, TS>(sm, my, head, 32, stail, s, X0, Y0, shaded, fsinv);
                 head += 32;
                 if (stail - shead >= 32) {
-                    wshade<S, TS>(sm, inv255, shead, 32, draws, f, s, X0, Y0, oobc);
+                    wshade<S, TS>(sm, my, inv255, shead, 32, draws, f, s, X0, Y0, oobc);
                     shead += 32;
                 }
             }
         }
-        if (tail != head) wdepth<S, TS>(sm, head, tail - head, stail, s, X0, Y0, shaded, fsinv);
+        if (tail != head) wdepth<S, TS>(sm, my, head, tail - head, stail, s, X0, Y0, shaded, fsinv);
         while (stail != shead) {
             const uint32_t nsh = min(stail - shead, 32u);
-            wshade<S, TS>(sm, inv255, shead, nsh, draws, f, s, X0, Y0, oobc);
+            wshade<S, TS>(sm, my, inv255, shead, nsh, draws, f, s, X0, Y0, oobc);
             shead += nsh;
         }
         __syncwarp();
@@ -470,7 +507,7 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
 // times nsx * nsx quadrants, taken one tile per warp from queue[4]; then bins without entries
 // from queue[1], like k_raster.
 template <int S, int TS>
-__global__ void __launch_bounds__(32 * kWarpUnitWarps) k_raster_warp(const FrameDev* __restrict__ frames,
+__global__ void __launch_bounds__(32 * kWarpUnitWarps, kWarpUnitCtas) k_raster_warp(const FrameDev* __restrict__ frames,
                                                                      int nframes,
                                                                      const uint32_t* __restrict__ order,
                                                                      uint32_t ntotal, uint32_t nsx,

@@ -139,6 +139,11 @@ class Renderer:
     def set_clear_depth(self, depth):
         check(_lib.load().rast_set_clear_depth(self._ctx, float(np.float32(depth))))
 
+    def set_heavy_tile_entries(self, min_entries):
+        """Bins with at least min_entries entries are rastered by a whole CTA per tile, the rest
+        by one warp per tile (0: all CTA-wide, the default; 0xFFFFFFFF: all by warps)."""
+        check(_lib.load().rast_set_heavy_tile_entries(self._ctx, int(min_entries)), "heavy tile entries")
+
     def upload(self, mesh):
         """Make a mesh resident (once per mesh object); returns its handle."""
         key = id(mesh)
@@ -232,9 +237,11 @@ class Renderer:
         return list(ms[:n])
 
 
-def render_scene(scene, tile=0, capture=False, log_capacity=0, renderer=None):
+def render_scene(scene, tile=0, capture=False, log_capacity=0, renderer=None, heavy_entries=None):
     """Render a scene dict (rusterizer_gb300.scenes) once; returns (argb, status, renderer)."""
     r = renderer or Renderer(scene["width"], scene["height"], scene.get("msaa", 4), tile=tile)
+    if heavy_entries is not None:
+        r.set_heavy_tile_entries(heavy_entries)
     if renderer is None:
         r.set_clear_depth(scene.get("clear_depth", np.finfo(np.float32).max))
         for i, t in enumerate(scene.get("textures", [])):

@@ -5,8 +5,9 @@ import oracle
 from rusterizer_gb300 import renderer, scenes
 
 
-def gpu_render(scene, tile=0, log_capacity=0):
-    argb, st, r = renderer.render_scene(scene, tile=tile, capture=True, log_capacity=log_capacity)
+def gpu_render(scene, tile=0, log_capacity=0, heavy_entries=None):
+    argb, st, r = renderer.render_scene(scene, tile=tile, capture=True, log_capacity=log_capacity,
+                                        heavy_entries=heavy_entries)
     depth, color = r.read_samples()
     stats = r.stats()
     log = r.log() if log_capacity else None
@@ -28,7 +29,7 @@ def channel_diff(a, b):
     return d
 
 
-def assert_parity(scene, tile=0, log=True, nthreads=1, colour_lsb=0, log_capacity=0):
+def assert_parity(scene, tile=0, log=True, nthreads=1, colour_lsb=0, log_capacity=0, heavy_entries=None):
     """Coverage (fragment log), depth-passed masks, per-sample depth and colour bit-exact;
     resolved ARGB within colour_lsb per channel (0 = bit-exact, the expected result).
     A log that reaches its capacity fails the test: both sides drop the rows past it, and the
@@ -36,7 +37,7 @@ def assert_parity(scene, tile=0, log=True, nthreads=1, colour_lsb=0, log_capacit
     cap = 0
     if log:
         cap = log_capacity or 4 * scenes.scene_triangles(scene) + 4 * scene["width"] * scene["height"]
-    ga, gd, gc, gs, gst, glog = gpu_render(scene, tile=tile, log_capacity=cap)
+    ga, gd, gc, gs, gst, glog = gpu_render(scene, tile=tile, log_capacity=cap, heavy_entries=heavy_entries)
     oa, od, oc, os_, ost, olog = oracle.render_scene(scene, nthreads=nthreads if not log else 1,
                                                      log_capacity=cap)
     if log:
