@@ -14,7 +14,10 @@
 // without entries. k_raster takes the heavy tiles.
 
 constexpr int kWarpUnitWarps = 4;  // warps (independent tiles) per CTA of k_raster_warp
-constexpr int kWarpUnitCtas = 5;   // CTAs per SM the launch bounds aim at
+// CTAs per SM the launch bounds aim at: with 4 samples the shared sample tiles allow 5; with
+// one sample 6 (79 registers, no spills; 7 spills and ran 2% slower on the scene mix, 5 3% slower)
+constexpr int kWarpUnitCtas = 5;
+constexpr int kWarpUnitCtas1 = 6;
 
 template <int S, int TS>
 struct alignas(16) WarpUnitSmem {
@@ -507,7 +510,7 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
 // times nsx * nsx quadrants, taken one tile per warp from queue[4]; then bins without entries
 // from queue[1], like k_raster.
 template <int S, int TS>
-__global__ void __launch_bounds__(32 * kWarpUnitWarps, kWarpUnitCtas) k_raster_warp(const FrameDev* __restrict__ frames,
+__global__ void __launch_bounds__(32 * kWarpUnitWarps, S == 1 ? kWarpUnitCtas1 : kWarpUnitCtas) k_raster_warp(const FrameDev* __restrict__ frames,
                                                                      int nframes,
                                                                      const uint32_t* __restrict__ order,
                                                                      uint32_t ntotal, uint32_t nsx,

@@ -91,3 +91,24 @@ def test_texture_out_of_bounds_warp_kernel():
 @pytest.mark.parametrize("heavy", SPLITS)
 def test_config1_full_size(heavy):
     assert_parity(scenes.config1(), log=False, nthreads=8, heavy_entries=heavy)
+
+
+@pytest.mark.parametrize("heavy", [0, ALL_WARP])
+@pytest.mark.parametrize("msaa", [4, 1])
+@pytest.mark.parametrize("tile", [8, 16, 32])
+@pytest.mark.parametrize("wh", [(1000, 300), (260, 70), (36, 20), (333, 217)])
+def test_tile_store_partial_tiles(heavy, msaa, tile, wh):
+    """Edge tiles that stick out of the frame on the right and at the bottom, with each raster
+    kernel: the warp kernel writes full tile rows with 16-byte stores when the frame's rows are
+    a multiple of 16 bytes (widths that are multiples of 4) and pixel by pixel otherwise (333
+    wide, and tiles past the right edge). Without the sample capture, which always takes the
+    pixel path, the image must equal the oracle's."""
+    import oracle
+    from rusterizer_gb300 import renderer
+    W, H = wh
+    s = scenes.soup_scene(1500, W, H, msaa, np.random.default_rng(W * 7 + H + tile), 64)
+    argb, st, r = renderer.render_scene(s, tile=tile, heavy_entries=heavy)
+    r.close()
+    oa, *_ = oracle.render_scene(s, nthreads=4)
+    assert st in (0, 6)
+    assert (argb == oa).all()
