@@ -387,27 +387,54 @@ __device__ __forceinline__ void warp_unit(WarpUnitSmem<S, TS>& sm, const float* 
             pos += take;
             if (take < 32) break;  // the batch is full, or the entries ran out
         }
-        // ---- B. candidates of each item (lane = item)
-        uint32_t c = 0, geo = 0;  // geo: x0 | y0 << 5 | w << 10 | h << 16 | trimmed << 21
+        // ---- B. candidates of each item (lane = item): the whole box, or for boxes of kTrimMin+
+        // columns each row trimmed by line_span
+        uint32_t c = 0, geo = 0, nrows = 0;  // geo: x0 | y0 << 5 | w << 10 | h << 16 | trimmed << 21
         if (lane < nit) {
             const uint32_t r = my.rect;
             const uint32_t x0 = r & 0xFFu, y0 = (r >> 8) & 0xFFu, x1 = (r >> 16) & 0xFFu, y1 = r >> 24;
             const uint32_t w = x1 - x0, h = y1 - y0;
-            if (w >= kTrimMin && h > 0) {
-                uint32_t run = 0;
-                for (uint32_t row = 0; row < h; ++row) {
-                    uint32_t a0 = x0, a1 = x1;
-                    line_span_pts<S, TS>(my.px, my.py, 0u, y0 + row, X0, Y0, a0, a1);
-                    sm.rsta[lane][row] = (uint8_t)a0;
-                    sm.rpre[lane][row] = (uint8_t)run;
-                    run += a1 - a0;
-                }
-                c = run;
-                geo = x0 | (y0 << 5) | (w << 10) | (h << 16) | (1u << 21);
-            } else {
-                c = w * h;
-                geo = x0 | (y0 << 5) | (w << 10) | (h << 16);
+            const bool trim = w >= kTrimMin && h > 0;
+            nrows = trim ? h : 0u;
+            c = w * h;
+            geo = x0 | (y0 << 5) | (w << 10) | (h << 16) | ((uint32_t)trim << 21);
+        }
+        // the rows to trim, spread over the lanes 32 at a time (a warp would otherwise run as many
+        // rounds as its tallest item has rows): task t is row t - (rows of earlier items) of the
+        // item whose running row count first exceeds t, read from that item's lane; the span's
+        // start goes to rsta, its length to rpre until the prefix pass below
+        const uint32_t rincl = warp_incl_scan(nrows);
+        const uint32_t rtot = __shfl_sync(0xFFFFFFFFu, rincl, 31);
+        for (uint32_t tb = 0; tb < rtot; tb += 32) {
+            const uint32_t t = tb + lane;
+            uint32_t j = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const uint32_t v = __shfl_sync(0xFFFFFFFFu, rincl, j + st - 1);
+                if (v <= t) j += st;
             }
+            j = min(j, 31u);
+            const float px[3] = {shfl_f(my.px[0], j), shfl_f(my.px[1], j), shfl_f(my.px[2], j)};
+            const float py[3] = {shfl_f(my.py[0], j), shfl_f(my.py[1], j), shfl_f(my.py[2], j)};
+            const uint32_t gj = __shfl_sync(0xFFFFFFFFu, geo, j);
+            const uint32_t row = t - __shfl_sync(0xFFFFFFFFu, rincl - nrows, j);
+            if (t < rtot) {
+                const uint32_t x0 = gj & 31u, y0 = (gj >> 5) & 31u;
+                uint32_t a0 = x0, a1 = x0 + ((gj >> 10) & 31u);
+                line_span_pts<S, TS>(px, py, 0u, y0 + row, X0, Y0, a0, a1);
+                sm.rsta[j][row] = (uint8_t)a0;
+                sm.rpre[j][row] = (uint8_t)(a1 - a0);
+            }
+        }
+        __syncwarp();
+        if (nrows) {
+            uint32_t run = 0;  // candidates before each row
+            for (uint32_t row = 0; row < nrows; ++row) {
+                const uint32_t len = sm.rpre[lane][row];
+                sm.rpre[lane][row] = (uint8_t)run;
+                run += len;
+            }
+            c = run;
         }
         const uint32_t incl = warp_incl_scan(c);
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
