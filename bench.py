@@ -31,7 +31,8 @@ sys.path.insert(0, ROOT)
 CONFIGS = {0: "cube 800x600 4xMSAA (12 tris)",
            1: "triangle soup 100k tris 1920x1080 4xMSAA",
            2: "heightfield 2M tris 3840x2160 4xMSAA"}
-MAX_TILES_PER_FRAME = 16384  # the library's per-frame bin limit (rast_types.h kMaxTilesPerFrame)
+COUNT_BAND_TILES = 16384  # bins counted in one pass (rast_types.h kCountBandTiles)
+MAX_TILES_PER_FRAME = 1 << 22  # the library's per-frame bin limit (rast_types.h kMaxTilesPerFrame)
 AUTO_BIG_BIN_TRIS = 8192  # from this many triangles the library picks 32-pixel bins (rast_internal.h)
 
 
@@ -40,12 +41,12 @@ def launches_per_frame(width, height, ntris, tile=0):
     builds the raster tile queue of a one-frame run), scatter, raster, plus the quadrant split
     when the frame uses 32-pixel bins (the library's automatic choice: 32-pixel bins for frames
     of AUTO_BIG_BIN_TRIS triangles or more, else 16, either one when the other would exceed
-    MAX_TILES_PER_FRAME bins)."""
-    def fits(t):
-        return -(-width // t) * -(-height // t) <= MAX_TILES_PER_FRAME
-    if not (tile in (8, 16, 32) and fits(tile)):
+    COUNT_BAND_TILES bins, and 32 for frames where both would)."""
+    def bins(t):
+        return -(-width // t) * -(-height // t)
+    if not (tile in (8, 16, 32) and bins(tile) <= MAX_TILES_PER_FRAME):
         order = (32, 16) if ntris >= AUTO_BIG_BIN_TRIS else (16, 32)
-        tile = next(t for t in order if fits(t))
+        tile = next((t for t in order if bins(t) <= COUNT_BAND_TILES), 32)
     return 8 if tile == 32 else 7
 
 

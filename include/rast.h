@@ -58,7 +58,9 @@ void rast_destroy(rast_ctx* ctx);
 /* Depth clear value; the reference uses f32::MAX (src/rasterizer/buffers.rs:6). */
 rast_status rast_set_clear_depth(rast_ctx* ctx, float depth);
 /* Screen tile edge in pixels (8, 16 or 32); 0 selects automatically: 32 for frames of 8192
- * triangles or more, else 16 (either one when the other would exceed 16384 tiles). */
+ * triangles or more, else 16 (either one when the other would exceed 16384 tiles, and 32 when
+ * both would). Frames of more than 16384 tiles are binned in several counting passes, one per
+ * 16384 tiles: any size rast_create accepts renders, large ones at some cost in binning. */
 rast_status rast_set_tile_size(rast_ctx* ctx, int tile);
 
 /* How raster tiles are split between the two raster kernels (no counterpart in the reference,

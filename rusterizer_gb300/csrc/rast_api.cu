@@ -49,11 +49,14 @@ int choose_tile(int w, int h, int msaa, int req, uint64_t ntris) {
     }
     (void)msaa;
     const bool big = ntris >= kAutoBigBinTris;
+    // the preferred size where one counting pass covers the frame's bins, else the other
     for (int ts : {big ? 32 : 16, big ? 16 : 32}) {
         long long n = (long long)((w + ts - 1) / ts) * ((h + ts - 1) / ts);
-        if (n <= kMaxTilesPerFrame) return ts;
+        if (n <= kCountBandTiles) return ts;
     }
-    return 0;
+    // larger frames: the fewest bins (one counting pass per band of them)
+    const long long n32 = (long long)((w + 31) / 32) * ((h + 31) / 32);
+    return n32 <= kMaxTilesPerFrame ? 32 : 0;
 }
 
 

@@ -351,35 +351,57 @@ __global__ void __launch_bounds__(256, 8) k_bin_count(const ChunkDev* __restrict
     pdl_enter();
     // per-bin counts of the chunk, two 16-bit counters per word (bin t in half t & 1 of word
     // t / 2): a chunk holds at most 8192 triangles, so no counter carries into its neighbour,
-    // and the histogram of 16384 bins takes 32 KB (8 CTAs per SM for the largest frames)
+    // and the histogram of kCountBandTiles = 16384 bins takes 32 KB (8 CTAs per SM for the
+    // largest frames). Frames with more bins are counted band by band: the first pass
+    // classifies the triangles and stores their boxes, later passes read the boxes back and
+    // count the bins of their band (rows of the box outside the band are skipped).
     extern __shared__ uint32_t hist[];
     const ChunkDev ch = chunks[blockIdx.x];
     const DrawDev& d = draws[ch.draw];
     const FrameDev& f = frames[d.frame];
     const uint32_t nt = f.ntiles, tx = f.tiles_x;
-    for (uint32_t t = threadIdx.x; t < (nt + 1) / 2; t += blockDim.x) hist[t] = 0;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < ch.tri_count; i += blockDim.x) {
-        const uint32_t tri = ch.tri_begin + i;
-        unsigned long long rect;
-        uint32_t aux;
-        classify_triangle(d, f, ch.draw, tri, ch.row, s, rect, aux);
-        const uint32_t g = f.rect_base + d.tbase + tri;
-        s.tri_rect[g] = rect;
-        s.tri_aux[g] = aux;
-        if (rect != kRectEmpty) {
-            uint32_t x0, y0, x1, y1;
-            tile_rect(rect, (uint32_t)f.ts, x0, y0, x1, y1);
-            for (uint32_t y = y0; y <= y1; ++y)
-                for (uint32_t x = x0; x <= x1; ++x) {
-                    const uint32_t t = y * tx + x;
-                    atomicAdd(&hist[t >> 1], (t & 1u) ? 0x10000u : 1u);
-                }
-        }
-    }
-    __syncthreads();
     uint32_t* row = s.counts + f.count_base + (unsigned long long)ch.row * nt;
-    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x) row[t] = (hist[t >> 1] >> ((t & 1u) * 16u)) & 0xFFFFu;
+    for (uint32_t b0 = 0; b0 < nt; b0 += (uint32_t)kCountBandTiles) {
+        const uint32_t b1 = min(nt, b0 + (uint32_t)kCountBandTiles);
+        for (uint32_t t = threadIdx.x; t < (b1 - b0 + 1) / 2; t += blockDim.x) hist[t] = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < ch.tri_count; i += blockDim.x) {
+            const uint32_t tri = ch.tri_begin + i;
+            const uint32_t g = f.rect_base + d.tbase + tri;
+            unsigned long long rect;
+            if (b0 == 0) {
+                uint32_t aux;
+                classify_triangle(d, f, ch.draw, tri, ch.row, s, rect, aux);
+                s.tri_rect[g] = rect;
+                s.tri_aux[g] = aux;
+            } else {
+                rect = s.tri_rect[g];  // stored by this thread in the first pass
+            }
+            if (rect != kRectEmpty) {
+                uint32_t x0, y0, x1, y1;
+                tile_rect(rect, (uint32_t)f.ts, x0, y0, x1, y1);
+                if (nt <= (uint32_t)kCountBandTiles) {  // one band: every bin of the box counts
+                    for (uint32_t y = y0; y <= y1; ++y)
+                        for (uint32_t x = x0; x <= x1; ++x) {
+                            const uint32_t t = y * tx + x;
+                            atomicAdd(&hist[t >> 1], (t & 1u) ? 0x10000u : 1u);
+                        }
+                } else {
+                    // rows of the box whose bins can fall in [b0, b1)
+                    const uint32_t ya = max(y0, b0 / tx), yb = min(y1, (b1 - 1) / tx);
+                    for (uint32_t y = ya; y <= yb; ++y)
+                        for (uint32_t x = x0; x <= x1; ++x) {
+                            const uint32_t t = y * tx + x;
+                            if (t >= b0 && t < b1) atomicAdd(&hist[(t - b0) >> 1], ((t - b0) & 1u) ? 0x10000u : 1u);
+                        }
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t t = b0 + threadIdx.x; t < b1; t += blockDim.x)
+            row[t] = (hist[(t - b0) >> 1] >> (((t - b0) & 1u) * 16u)) & 0xFFFFu;
+        if (b1 < nt) __syncthreads();  // the histogram is cleared again for the next band
+    }
 }
 
 // ===================================================================== binning: scans
@@ -1806,7 +1828,8 @@ cudaError_t launch_bin_count(const LaunchArgs& a) {
     // smaller value set by another host thread must not undercut a concurrent larger launch
     static std::mutex mu;
     static int configured[kMaxDevices] = {};
-    const int bytes = (int)(((a.max_tiles + 1) / 2) * sizeof(uint32_t));
+    const uint32_t band = a.max_tiles < (uint32_t)kCountBandTiles ? a.max_tiles : (uint32_t)kCountBandTiles;
+    const int bytes = (int)(((band + 1) / 2) * sizeof(uint32_t));
     const int dev = current_device();
     if (dev < 0) return cudaErrorInvalidDevice;
     {

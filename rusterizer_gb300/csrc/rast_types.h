@@ -30,7 +30,11 @@ constexpr float kCullEps = 0.000001f;          // src/rasterizer/clipping.rs:12
 constexpr int kMaxPoly = 32;                   // clip polygon capacity (a convex clip needs 9)
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kRectEmpty = ~0ull;
-constexpr int kMaxTilesPerFrame = 16384;       // per-frame tile count limit (smem histograms)
+// bins of one frame: up to kCountBandTiles are counted in one pass over a chunk's triangles
+// (a 32 KB shared histogram); larger frames (any 16384 x 16384 frame fits) take one pass per
+// band of kCountBandTiles bins, so the automatic bin size avoids them where it can
+constexpr int kCountBandTiles = 16384;
+constexpr int kMaxTilesPerFrame = 1 << 22;
 // Raster tile queue counters per (msaa, tile) launch group: [0] heavy-tile tickets, [1] empty-bin
 // tickets, [2] bins with entries, [3] heavy bins, [4] light-tile tickets
 constexpr int kQueueSlots = 8;

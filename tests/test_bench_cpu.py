@@ -17,13 +17,14 @@ def bench():
 
 
 def test_launches_per_frame_follows_the_bin_size(bench):
-    # 8 kernels with 16-pixel bins, 9 with 32-pixel bins (the quadrant split)
+    # 7 kernels with 16-pixel bins, 8 with 32-pixel bins (the quadrant split)
     assert bench.launches_per_frame(800, 600, 12) == 7            # cube: few triangles, 16-pixel
     assert bench.launches_per_frame(1920, 1080, 100_000) == 8     # soup: 32-pixel from 8192 tris
     assert bench.launches_per_frame(1920, 1080, 8191) == 7
     assert bench.launches_per_frame(3840, 2160, 12) == 8          # 16-pixel bins would exceed 16384
     assert bench.launches_per_frame(1920, 1080, 100_000, tile=16) == 7
-    assert bench.launches_per_frame(3840, 2160, 100, tile=16) == 8  # forced size that cannot fit
+    assert bench.launches_per_frame(3840, 2160, 100, tile=16) == 7  # asked for: two counting bands
+    assert bench.launches_per_frame(16384, 16384, 100) == 8        # beyond one band either way: 32
     assert bench.launches_per_frame(256, 256, 100, tile=32) == 8
 
 

@@ -108,3 +108,21 @@ def test_depth_ties_keep_first_writer():
     z = np.full(len(tris), np.float32(0.25), np.float32)
     s = grid_scene(tris, fs=scenes.FS_COLOR, z=z, seed=9)
     assert_parity(s, tile=16)
+
+
+@pytest.mark.parametrize("W,H,msaa,ntris,tile", [
+    (8192, 4320, 4, 20000, 0),     # 256 x 135 = 34 560 bins of 32 pixels: three counting bands
+    (16384, 16384, 1, 3000, 0),    # the largest frame: 262 144 bins, sixteen bands
+    (4100, 4100, 4, 6000, 16),     # 16-pixel bins asked for: 66 049 bins, five bands
+])
+def test_frames_beyond_one_counting_band(W, H, msaa, ntris, tile):
+    """Frames with more bins than one counting pass covers are counted band by band; the image
+    must equal the oracle's like any other frame (no sample capture at these sizes)."""
+    import oracle
+    from rusterizer_gb300 import renderer
+    s = scenes.soup_scene(ntris, W, H, msaa, np.random.default_rng(W + H + msaa), 64)
+    argb, st, r = renderer.render_scene(s, tile=tile)
+    r.close()
+    assert st in (0, 6), st
+    oa, *_ = oracle.render_scene(s, nthreads=8)
+    assert (argb == oa).all()
