@@ -6,7 +6,8 @@ textured fragment shader over a 2048x2048 checkerboard, viewed at 45 degrees so 
 are subpixel. One step is one full frame: vertex stage, clipping/setup, order-preserving
 binning, per-tile raster and resolve. Inputs (mesh, texture) are resident in HBM for `value`; `e2e` streams the mesh from
 pinned host memory through rast_mesh_update and reads the image back every step, from two host
-threads with a context each so that copies overlap kernels (`one_thread_value`: one thread).
+threads with a context each so that copies overlap kernels (`one_thread_value`: one thread;
+`one_thread_pipelined_value`: one thread with asynchronous mesh updates and image readbacks).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config 0|1|2|3|4] [--impl ours|reference]
 
@@ -507,15 +508,18 @@ def run_ours(args):
                 self.step()
 
     class PipelinedLane(E2ELane):
-        """One host thread, two resident meshes used in turn: each step streams the next step's
-        mesh with rast_mesh_update_async (its copies overlap the current frame) and renders the
-        current mesh into pinned host memory with rast_framebuffer."""
+        """One host thread, two resident meshes and two pinned images used in turn: each step
+        streams the next step's mesh with rast_mesh_update_async (its copies overlap the current
+        frame), enqueues the current frame into pinned host memory with rast_framebuffer_async
+        (its copy overlaps the next frame) and waits for the previous frame's image with
+        rast_wait_output. The first step is synchronous (it sizes the context's capacities)."""
 
         def __init__(self):
             super().__init__()
             self.m2 = renderer.Mesh(d0["pos"], d0["uv"], d0["idx"])
             self.handles = [self.mh, self.r.upload(self.m2)]
             self.meshes = [self.m, self.m2]
+            self.outs = [self.out, torch.empty(W * H, dtype=torch.int32).pin_memory()]
             self.k = 0
 
         def step(self):
@@ -525,9 +529,19 @@ def run_ours(args):
                                          ctypes.cast(self.nidx.data_ptr(), u32p))
             assert s == 0, s
             self.r.render(self.meshes[self.k % 2], renderer.VS_MVP, d0.get("fs", 0))
-            s = L.rast_framebuffer(self.r._ctx, ctypes.c_void_p(self.out.data_ptr()))
+            out = ctypes.c_void_p(self.outs[self.k % 2].data_ptr())
+            if self.k == 0:
+                s = L.rast_framebuffer(self.r._ctx, out)
+            else:
+                s = L.rast_framebuffer_async(self.r._ctx, out)
+                assert s == 0, s
+                s = L.rast_wait_output(self.r._ctx, ctypes.c_void_p(self.outs[(self.k - 1) % 2].data_ptr()))
             assert s == 0, s
             self.k += 1
+
+        def run(self, n):
+            super().run(n)
+            assert L.rast_wait_output(self.r._ctx, None) == 0
 
     lanes = [E2ELane() for _ in range(2)]
     piped = PipelinedLane()
@@ -564,7 +578,8 @@ def run_ours(args):
     queue()
     ref_img = r.framebuffer()
     for ln in lanes + [piped]:
-        assert (ln.out.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
+        for o in getattr(ln, "outs", [ln.out]):
+            assert (o.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
     h2d = lanes[0].npos.numel() * 4 + lanes[0].nuv.numel() * 4 + lanes[0].nidx.numel() * 4
     for ln in lanes + [piped]:
         ln.r.close()

@@ -113,9 +113,18 @@ rast_status rast_draw(rast_ctx* ctx, rast_mesh mesh, int vs_id, int fs_id);
 rast_status rast_framebuffer(rast_ctx* ctx, uint32_t* argb_out);
 
 /* Same frame, enqueued on the context stream without waiting: no overflow re-run and no
- * status readback (capacities come from earlier rast_framebuffer calls). argb_out must be a
- * device pointer or NULL. Used by throughput loops; no counterpart in the reference. */
-rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out_device);
+ * status readback (capacities come from earlier rast_framebuffer calls). argb_out is a device
+ * pointer (the frame writes it), NULL, or host memory: the frame then resolves into one of two
+ * staging buffers in turn, and a side stream copies it to argb_out once the frame is done, so
+ * that one host thread's next frame renders while this one is copied. Page-locked host memory
+ * makes that copy asynchronous. The host image is complete after rast_wait_output(ctx,
+ * argb_out) (or any synchronous call of the context). Used by throughput loops; no counterpart
+ * in the reference. */
+rast_status rast_framebuffer_async(rast_ctx* ctx, uint32_t* argb_out);
+
+/* Waits until the asynchronous copies into host array argb_out (every one when NULL) enqueued
+ * by rast_framebuffer_async have landed. */
+rast_status rast_wait_output(rast_ctx* ctx, const uint32_t* argb_out);
 
 /* One frame of one mesh that allocates nothing. No counterpart in the reference: it is for
  * callers that cannot allocate device memory when they render (an engine or plugin host that

@@ -43,6 +43,7 @@ SIGNATURES = {
     "rast_draw": (_i, [_vp, _u32, _i, _i]),
     "rast_framebuffer": (_i, [_vp, _vp]),
     "rast_framebuffer_async": (_i, [_vp, _vp]),
+    "rast_wait_output": (_i, [_vp, _vp]),
     "rast_render_noalloc": (_i, [_i, _i, _i, _i, _c.c_float, _vp, _vp, _vp, _u32, _vp, _u32,
                                  _fp, _fp, _fp, _vp, _i, _i, _i, _vp, _vp]),
     "rast_render_batch": (_i, [_vp, _vp, _u32]),

@@ -384,8 +384,12 @@ rast_ctx* rast_create(int width, int height, int msaa, rast_status* status) {
 void rast_destroy(rast_ctx* c) {
     if (!c) return;
     c->sync_copies();
+    c->sync_readbacks();
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->frame_done) cudaEventDestroy(c->frame_done);
+    if (c->readback) cudaStreamDestroy(c->readback);
+    for (cudaEvent_t e : c->rb_done)
+        if (e) cudaEventDestroy(e);
     cudaStreamSynchronize(c->E.stream);
     for (MeshRec& m : c->meshes) m.release();
     for (TexRec& t : c->textures) t.release();
@@ -549,7 +553,28 @@ static rast_status framebuffer_impl(rast_ctx* c, uint32_t* argb_out, bool sync) 
         }
         cudaGetLastError();
     }
-    if (!direct && !c->out.reserve(npx)) return RAST_OOM;
+    // an asynchronous frame into host memory resolves into a staging buffer of its own and is
+    // copied on the readback stream; a synchronous one first lets earlier readbacks land
+    const bool host_async = !sync && argb_out && !direct;
+    const unsigned slot = c->rb_next;
+    if (host_async) {
+        if (!c->readback && cudaStreamCreateWithFlags(&c->readback, cudaStreamNonBlocking) != cudaSuccess) {
+            c->readback = nullptr;
+            return RAST_CUDA_ERROR;
+        }
+        for (cudaEvent_t* e : {&c->rb_done[0], &c->rb_done[1], &c->frame_done})
+            if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+                *e = nullptr;
+                return RAST_CUDA_ERROR;
+            }
+        if (!c->rb_stage[slot].reserve(npx)) return RAST_OOM;
+        // the staging buffer's previous copy must have read it before this frame resolves
+        if (c->rb_pending[slot] && cudaStreamWaitEvent(c->E.stream, c->rb_done[slot], 0) != cudaSuccess)
+            return RAST_CUDA_ERROR;
+    } else if (sync) {
+        c->sync_readbacks();
+    }
+    if (!direct && !host_async && !c->out.reserve(npx)) return RAST_OOM;
     if (c->capture && (!c->dbg_depth.reserve(npx * c->msaa) || !c->dbg_color.reserve(npx * c->msaa)))
         return RAST_OOM;
     std::vector<FrameJob> jobs(1);
@@ -559,7 +584,7 @@ static rast_status framebuffer_impl(rast_ctx* c, uint32_t* argb_out, bool sync) 
     J.msaa = c->msaa;
     J.ts = ts;
     J.clear_depth = c->clear_depth;
-    J.out_dev = direct ? direct : c->out.p;
+    J.out_dev = direct ? direct : host_async ? c->rb_stage[slot].p : c->out.p;
     J.dbg_depth = c->capture ? c->dbg_depth.p : nullptr;
     J.dbg_color = c->capture ? c->dbg_color.p : nullptr;
     J.draws = c->queue;
@@ -591,7 +616,17 @@ static rast_status framebuffer_impl(rast_ctx* c, uint32_t* argb_out, bool sync) 
     if (c->frame_done && cudaEventRecord(c->frame_done, c->E.stream) == cudaSuccess) c->frame_recorded = true;
     if (s != RAST_OK && s != RAST_TEXTURE_OOB) return s;
     if (sync && J.need) c->bin_hint = std::max<uint64_t>(c->bin_hint, J.need + J.need / 8);
-    if (argb_out && !direct) {
+    if (host_async) {
+        // the copy waits for this frame (frame_done was recorded right after it)
+        if (!c->frame_recorded || cudaStreamWaitEvent(c->readback, c->frame_done, 0) != cudaSuccess ||
+            cudaMemcpyAsync(argb_out, c->rb_stage[slot].p, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            c->readback) != cudaSuccess ||
+            cudaEventRecord(c->rb_done[slot], c->readback) != cudaSuccess)
+            return RAST_CUDA_ERROR;
+        c->rb_dst[slot] = argb_out;
+        c->rb_pending[slot] = true;
+        c->rb_next = slot ^ 1u;
+    } else if (argb_out && !direct) {
         if (cudaMemcpyAsync(argb_out, c->out.p, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             c->E.stream) != cudaSuccess)
             return RAST_CUDA_ERROR;
@@ -604,8 +639,18 @@ rast_status rast_framebuffer(rast_ctx* c, uint32_t* argb_out) { return framebuff
 
 /* Enqueue-only variant used by throughput loops: no stream synchronisation and no overflow
  * re-run; capacities come from earlier synchronous frames of the same context. */
-rast_status rast_framebuffer_async(rast_ctx* c, uint32_t* argb_out_device) {
-    return framebuffer_impl(c, argb_out_device, false);
+rast_status rast_framebuffer_async(rast_ctx* c, uint32_t* argb_out) {
+    return framebuffer_impl(c, argb_out, false);
+}
+
+rast_status rast_wait_output(rast_ctx* c, const uint32_t* argb_out) {
+    if (!c) return RAST_INVALID_ARG;
+    for (unsigned k = 0; k < 2; ++k) {
+        if (!c->rb_pending[k] || (argb_out && c->rb_dst[k] != argb_out)) continue;
+        if (cudaEventSynchronize(c->rb_done[k]) != cudaSuccess) return RAST_CUDA_ERROR;
+        c->rb_pending[k] = false;
+    }
+    return RAST_OK;
 }
 
 rast_status rast_stats(rast_ctx* c, uint64_t* shaded, uint64_t* fsinv, uint64_t* oob) {

@@ -296,4 +296,20 @@ struct rast_ctx {
         if (copy) cudaStreamSynchronize(copy);
         for (rast::MeshRec& m : meshes) m.pending = false;
     }
+    // asynchronous frames into host memory: a frame resolves into staging buffer rb_next
+    // (alternating), which `readback` copies to the host once the frame is done; a staging
+    // buffer is written again only after its previous copy (rb_done). rb_dst/rb_pending name
+    // each buffer's last copy for rast_wait_output.
+    rast::DevBuf<uint32_t> rb_stage[2];
+    cudaStream_t readback = nullptr;
+    cudaEvent_t rb_done[2] = {nullptr, nullptr};
+    const void* rb_dst[2] = {nullptr, nullptr};
+    bool rb_pending[2] = {false, false};
+    unsigned rb_next = 0;
+    // waits for every asynchronous readback (before synchronous frames, which could otherwise
+    // be overtaken by an earlier frame's copy into the same host array)
+    void sync_readbacks() {
+        if (readback) cudaStreamSynchronize(readback);
+        rb_pending[0] = rb_pending[1] = false;
+    }
 };

@@ -64,3 +64,55 @@ def test_async_updates_of_two_meshes_in_turn():
         img = out.numpy().view(np.uint32).reshape(H, W)
         assert (img == refs[order[k]]).all(), (k, order[k])
     r.close()
+
+
+def test_async_frames_into_host_memory():
+    """rast_framebuffer_async into host arrays: each frame resolves into one of two staging
+    buffers and is copied on a side stream while the next frame renders. Every image must equal
+    the synchronous frame of the same view once rast_wait_output returns, in pinned and pageable
+    memory, and a synchronous frame into the same array afterwards must not be overwritten by
+    an earlier frame's late copy."""
+    torch = pytest.importorskip("torch")
+    from rusterizer_gb300 import math as rm
+    s = scenes.small_soup(5, ntris=3000)
+    H, W = s["height"], s["width"]
+    L = _lib.load()
+    r = renderer.Renderer(W, H, s["msaa"])
+    r.uniforms().bind_texture(0, renderer.Texture(s["textures"][0]))
+    blk = r.uniforms().write_block()
+    blk.view, blk.projection = s["view"], s["proj"]
+    d = s["draws"][0]
+    worlds = [rm.mat4_mul(rm.translate(np.float32(0.05 * k), 0.0, 0.0), d["world"]) for k in range(7)]
+
+    def frame(k):
+        blk.world = worlds[k]
+        r.render(d, renderer.VS_MVP, d.get("fs", 0))
+
+    want = []
+    for k in range(len(worlds)):
+        frame(k)
+        want.append(r.framebuffer().copy())  # synchronous: also sizes the context's capacities
+    assert len({w.tobytes() for w in want}) == len(want)  # the views differ
+    pinned = [torch.zeros(W * H, dtype=torch.int32).pin_memory() for _ in range(2)]
+    pageable = [np.zeros(W * H, np.uint32) for _ in range(2)]
+    for outs, ptr in ((pinned, lambda o: o.data_ptr()), (pageable, lambda o: o.ctypes.data)):
+        for k in range(len(worlds)):
+            frame(k)
+            assert L.rast_framebuffer_async(r._ctx, ctypes.c_void_p(ptr(outs[k % 2]))) == _lib.OK
+            if k:
+                prev = outs[(k - 1) % 2]
+                assert L.rast_wait_output(r._ctx, ctypes.c_void_p(ptr(prev))) == _lib.OK
+                got = prev.numpy() if hasattr(prev, "numpy") else prev
+                assert (got.view(np.uint32).reshape(H, W) == want[k - 1]).all(), k - 1
+        assert L.rast_wait_output(r._ctx, None) == _lib.OK
+        last = outs[(len(worlds) - 1) % 2]
+        got = last.numpy() if hasattr(last, "numpy") else last
+        assert (got.view(np.uint32).reshape(H, W) == want[-1]).all()
+    # an asynchronous frame, then a synchronous one into the same host array
+    frame(0)
+    assert L.rast_framebuffer_async(r._ctx, ctypes.c_void_p(pinned[0].data_ptr())) == _lib.OK
+    frame(3)
+    assert L.rast_framebuffer(r._ctx, ctypes.c_void_p(pinned[0].data_ptr())) == _lib.OK
+    assert (pinned[0].numpy().view(np.uint32).reshape(H, W) == want[3]).all()
+    r.close()
+    assert (want[0] == oracle.render_scene(dict(s, draws=[dict(d, world=worlds[0])]))[0]).all()
