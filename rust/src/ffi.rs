@@ -72,7 +72,17 @@ extern "C" {
     pub fn rast_texture_upload(ctx: *mut rast_ctx, slot: c_int, rgba8: *const u8, w: c_int, h: c_int) -> rast_status;
     pub fn rast_set_uniforms(ctx: *mut rast_ctx, world: *const f32, view: *const f32, proj: *const f32) -> rast_status;
     pub fn rast_draw(ctx: *mut rast_ctx, mesh: rast_mesh, vs_id: c_int, fs_id: c_int) -> rast_status;
+    pub fn rast_mesh_update_async(
+        ctx: *mut rast_ctx,
+        mesh: rast_mesh,
+        pos: *const f32,
+        uv: *const f32,
+        rgba: *const f32,
+        idx: *const u32,
+    ) -> rast_status;
     pub fn rast_framebuffer(ctx: *mut rast_ctx, argb_out: *mut u32) -> rast_status;
+    pub fn rast_framebuffer_async(ctx: *mut rast_ctx, argb_out: *mut u32) -> rast_status;
+    pub fn rast_wait_output(ctx: *mut rast_ctx, argb_out: *const u32) -> rast_status;
     pub fn rast_render_batch(ctx: *mut rast_ctx, scenes: *const rast_scene, n: u32) -> rast_status;
     pub fn rast_stats(
         ctx: *mut rast_ctx,
