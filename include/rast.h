@@ -195,7 +195,10 @@ rast_status rast_autotune_batch(rast_ctx* ctx, const rast_scene* scenes, uint32_
                                 int best_tiles[2]);
 
 /* A batch captured into a CUDA graph once (after one sizing run) and re-rendered by one graph
- * launch per call. argb_out pointers must be device pointers. The batch owns its own scratch
+ * launch per call. argb_out pointers are device pointers or page-locked host memory (the graph
+ * then resolves those scenes into the batch's own staging buffer and copies them out at its
+ * end; pageable host memory is refused with RAST_INVALID_ARG). Two batches launched in turn
+ * without waiting overlap one's copies with the other's kernels. The batch owns its own scratch
  * and stream; the context's meshes and textures must outlive it. */
 typedef struct rast_batch rast_batch;
 rast_status rast_batch_create(rast_ctx* ctx, const rast_scene* scenes, uint32_t n, rast_batch** out);

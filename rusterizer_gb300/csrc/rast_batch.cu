@@ -29,6 +29,14 @@ bool is_device_ptr(const void* p) {
     return dev;
 }
 
+// Page-locked (or registered) host memory: the only host memory a captured copy may write.
+bool is_pinned_host_ptr(const void* p) {
+    cudaPointerAttributes attr;
+    const bool pinned = cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    return pinned;
+}
+
 int scene_tile(const rast_ctx* c, const rast_scene& s) {
     int req = s.tile;
     if (req == 0) req = c->tuned_tile[s.msaa == 4 ? 1 : 0];
@@ -113,9 +121,28 @@ struct rast_batch {
     rast_ctx* ctx = nullptr;
     Engine E;
     std::vector<FrameJob> jobs;
+    DevBuf<uint32_t> stage;          // resolved images of the scenes with host outputs
+    std::vector<size_t> host_off;    // per scene: its offset in `stage`, or -1 (device output)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
+
+namespace {
+
+// The batch's copies of its staged images to the scenes' host outputs, on its stream (one
+// chain of copies: spreading them over four parallel graph branches did not move more bytes).
+bool enqueue_host_copies(rast_batch* b, const rast_scene* sc, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->host_off[i] == (size_t)-1) continue;
+        const size_t bytes = (size_t)sc[i].width * sc[i].height * sizeof(uint32_t);
+        if (cudaMemcpyAsync(sc[i].argb_out, b->stage.p + b->host_off[i], bytes, cudaMemcpyDeviceToHost,
+                            b->E.stream) != cudaSuccess)
+            return false;
+    }
+    return true;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -273,7 +300,15 @@ rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, ras
     if (!b) return RAST_OOM;
     b->ctx = c;
     c->sync_copies();
-    rast_status st = build_jobs(c, sc, n, false, b->jobs, nullptr, nullptr);
+    size_t staging = 0;
+    rast_status st = build_jobs(c, sc, n, true, b->jobs, &b->host_off, &staging);
+    // host outputs: page-locked only (the graph copies into them); resolved into the batch's
+    // own staging buffer
+    for (uint32_t i = 0; st == RAST_OK && i < n; ++i)
+        if (b->host_off[i] != (size_t)-1 && !is_pinned_host_ptr(sc[i].argb_out)) st = RAST_INVALID_ARG;
+    if (st == RAST_OK && staging && !b->stage.reserve(staging)) st = RAST_OOM;
+    for (uint32_t i = 0; st == RAST_OK && i < n; ++i)
+        if (b->host_off[i] != (size_t)-1) b->jobs[i].out_dev = b->stage.p + b->host_off[i];
     if (st == RAST_OK && !b->E.init()) st = RAST_CUDA_ERROR;
     // the context's (autotuned) raster settings
     for (int k = 0; k < 2; ++k) {
@@ -293,6 +328,7 @@ rast_status rast_batch_create(rast_ctx* c, const rast_scene* sc, uint32_t n, ras
             st = RAST_CUDA_ERROR;
         } else {
             rast_status rs = run_frames(b->E, b->jobs);
+            if (rs == RAST_OK && !enqueue_host_copies(b, sc, n)) rs = RAST_CUDA_ERROR;
             cudaMemcpyAsync(b->E.h_state, b->E.d_state, sizeof(DeviceState), cudaMemcpyDeviceToHost,
                             b->E.stream);
             cudaGraph_t g = nullptr;

@@ -73,3 +73,44 @@ def test_graph_batch_replays_identically_and_autotune():
             img = d.cpu().numpy().view(np.uint32).reshape(s["height"], s["width"])
             assert (img == ref).all(), (rep, s["name"])
     br.close()
+
+
+def test_graph_batches_with_host_outputs_in_turn():
+    """Captured batches writing page-locked host memory (half the scenes) and device memory
+    (the other half), two of them launched in turn without waiting so that one's copies overlap
+    the other's kernels: after each is waited for, every image equals the oracle's. Pageable
+    host outputs are refused (a graph cannot copy into them)."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from rusterizer_gb300 import _lib
+    sc = mixed_scenes()
+    refs = [oracle.render_scene(s)[0] for s in sc]
+    br = BatchRenderer()
+    for s in sc:
+        br.add_scene(s)
+    sets = []
+    for _ in range(2):
+        outs = []
+        for i, s in enumerate(sc):
+            n = s["height"] * s["width"]
+            outs.append(torch.zeros(n, dtype=torch.int32).pin_memory() if i % 2 == 0
+                        else torch.zeros(n, dtype=torch.int32, device="cuda"))
+        sets.append(outs)
+    graphs = [br.capture([o.data_ptr() for o in outs]) for outs in sets]
+    for rep in range(3):
+        for outs in sets:
+            for o in outs:
+                o.zero_()
+        torch.cuda.synchronize()
+        for g in graphs:
+            BatchRenderer.replay(g, wait=False)
+        for g, outs in zip(graphs, sets):
+            torch.cuda.ExternalStream(BatchRenderer.graph_stream(g)).synchronize()
+            for s, o, ref in zip(sc, outs, refs):
+                img = o.cpu().numpy().view(np.uint32).reshape(s["height"], s["width"])
+                assert (img == ref).all(), (rep, s["name"])
+    pageable = [np.zeros(s["height"] * s["width"], np.uint32) for s in sc]
+    arr = br._array([o.ctypes.data for o in pageable], list(range(len(sc))))
+    h = ctypes.c_void_p()
+    assert _lib.load().rast_batch_create(br._ctx, arr, len(sc), ctypes.byref(h)) == _lib.INVALID_ARG
+    br.close()
