@@ -126,3 +126,34 @@ def test_frames_beyond_one_counting_band(W, H, msaa, ntris, tile):
     assert st in (0, 6), st
     oa, *_ = oracle.render_scene(s, nthreads=8)
     assert (argb == oa).all()
+
+
+def nonfinite_scene(fs, seed=3):
+    """A soup with NaN, +-inf and +-1e30 (infinite after the transform) in vertex positions,
+    texture coordinates and vertex colours."""
+    s = scenes.small_soup(61 + fs, ntris=1500, fs=fs)
+    d = s["draws"][0]
+    pos, uv, rgba = d["pos"].copy(), d["uv"].copy(), d["rgba"].copy()
+    rng = np.random.default_rng(seed)
+    n = len(pos)
+    for val in (np.nan, np.inf, -np.inf, 1e30, -1e30):
+        i = rng.choice(n, 12, replace=False)
+        pos[i, rng.integers(0, 3, 12)] = val
+    for val in (np.nan, np.inf, -np.inf, 1e30):
+        i = rng.choice(n, 20, replace=False)
+        uv[i, rng.integers(0, 2, 20)] = val
+        i = rng.choice(n, 20, replace=False)
+        rgba[i, rng.integers(0, 4, 20)] = val
+    d.update(pos=pos.astype(np.float32), uv=uv.astype(np.float32), rgba=rgba.astype(np.float32))
+    return s
+
+
+@pytest.mark.parametrize("heavy", [None, 0xFFFFFFFF])
+@pytest.mark.parametrize("tile", [16, 32])
+@pytest.mark.parametrize("fs", [scenes.FS_TEXTURE, scenes.FS_COLOR, scenes.FS_DEBUG])
+def test_nonfinite_inputs(fs, tile, heavy):
+    """Non-finite inputs take the reference's paths: f32::min/max skip NaN in the box,
+    saturating casts send NaN to 0 and infinities to the ends, comparisons with NaN fail (the
+    edge tie rule, the clip tests, the depth test), clamp passes NaN, and texels past the
+    texture are reported. Coverage, depth, samples, image and counts equal the oracle's."""
+    assert_parity(nonfinite_scene(fs), tile=tile, log_capacity=4_000_000, heavy_entries=heavy)
