@@ -157,3 +157,27 @@ def test_nonfinite_inputs(fs, tile, heavy):
     edge tie rule, the clip tests, the depth test), clamp passes NaN, and texels past the
     texture are reported. Coverage, depth, samples, image and counts equal the oracle's."""
     assert_parity(nonfinite_scene(fs), tile=tile, log_capacity=4_000_000, heavy_entries=heavy)
+
+
+@pytest.mark.parametrize("heavy", [None, 0xFFFFFFFF])
+@pytest.mark.parametrize("msaa", [4, 1])
+@pytest.mark.parametrize("wh", [(1, 1), (1, 300), (300, 1), (17, 9), (33, 65)])
+def test_degenerate_frame_shapes(wh, msaa, heavy):
+    """Frames of one pixel, one row, one column and sizes below one bin: partial tiles on
+    every side, bins that hold a single pixel."""
+    W, H = wh
+    s = scenes.soup_scene(400, W, H, msaa, np.random.default_rng(W * 31 + H), 16)
+    assert_parity(s, log_capacity=4_000_000, heavy_entries=heavy)
+
+
+def test_empty_meshes_between_draws():
+    """Meshes with no triangles (and no vertices) drawn between other draws: they add nothing
+    and the draws around them keep their submission order."""
+    base = scenes.small_soup(71, ntris=600)
+    d = base["draws"][0]
+    empty = {"pos": np.zeros((0, 3), np.float32), "uv": np.zeros((0, 2), np.float32),
+             "rgba": np.zeros((0, 4), np.float32), "idx": np.zeros((0, 3), np.uint32),
+             "world": d["world"], "fs": scenes.FS_TEXTURE}
+    shifted = dict(d, world=rm.mat4_mul(rm.translate(0.1, 0.0, 0.0), d["world"]), fs=scenes.FS_COLOR)
+    s = dict(base, draws=[empty, d, empty, shifted, empty])
+    assert_parity(s)
