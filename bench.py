@@ -882,7 +882,7 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--nscenes", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+",
-                    default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 12000, 16000, 20000, 24000, 32000])
+                    default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 12000, 14000, 16000, 18000, 20000, 24000, 32000])
     ap.add_argument("--seconds", type=float, default=1.0)
     ap.add_argument("--p99-bound-ms", type=float, default=50.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
