@@ -802,7 +802,7 @@ def run_serving(args):
             # one request per launch gains nothing from the warp-per-tile kernel (too few tiles
             # per launch): the plain server runs every bin CTA-wide, the library default
             L.rast_set_heavy_tile_entries(br._ctx, 0)
-        srv = RenderServer(br, budget_bytes=40 << 30, streams=2, one_per_launch=(mode == "plain"))
+        srv = RenderServer(br, budget_bytes=40 << 30, streams=args.streams, one_per_launch=(mode == "plain"))
         poisson_run(srv, len(sc), outs, 2000.0, 0.5, rng)  # warm-up: sizes every buffer
         sweep = []
         sampler = ClockSampler(local) if mode == "batched" else None
@@ -819,8 +819,14 @@ def run_serving(args):
             sampler.__exit__(None, None, None)
             clk = sampler.summary()
         srv.close()
-        ok = [s for s in sweep if s["p99_ms"] <= bound]
-        best = max(ok, key=lambda s: s["req_per_s"]) if ok else None
+        # the sustained rate: the highest offered rate of the sweep's passing prefix (a rate past
+        # saturation can pass a one-second window by luck after a lower one failed)
+        ok = []
+        for st_ in sweep:
+            if st_["p99_ms"] > bound:
+                break
+            ok.append(st_)
+        best = ok[-1] if ok else None
         results[mode] = {"sweep": sweep, "max_rate_within_bound": best["offered_rate"] if best else 0.0,
                          "at_max": best}
     br.close()
@@ -854,7 +860,7 @@ def run_serving(args):
             "ms_per_step": 1000.0 * args.seconds, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": batch_config(4, sc, world), "p99_bound_ms": bound, "autotune": tuned,
-            "hbm_budget_bytes": 40 << 30, "streams": 2,
+            "hbm_budget_bytes": 40 << 30, "streams": args.streams,
             "p50_ms": at.get("p50_ms"), "p99_ms": at.get("p99_ms"), "mean_batch": at.get("mean_batch"),
             "plain_max_rate_within_bound": p["max_rate_within_bound"],
             "batched_vs_plain": (b["max_rate_within_bound"] / p["max_rate_within_bound"]
@@ -884,6 +890,7 @@ def main():
     ap.add_argument("--rates", type=float, nargs="+",
                     default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 12000, 14000, 16000, 18000, 20000, 24000, 32000])
     ap.add_argument("--seconds", type=float, default=1.0)
+    ap.add_argument("--streams", type=int, default=3, help="serving: launch slots of each server")
     ap.add_argument("--p99-bound-ms", type=float, default=50.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tile", type=int, default=0)
