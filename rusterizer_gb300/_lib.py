@@ -102,8 +102,8 @@ def load():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise RuntimeError("librast.so is not built (run rusterizer_gb300/build.py or "
-                               "__graft_entry__.build()); there is no CPU fallback")
+            raise RuntimeError("librast.so is not built (run python rusterizer_gb300/build.py); "
+                               "there is no CPU fallback")
         L = ctypes.CDLL(LIB_PATH)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name, None)
