@@ -182,10 +182,11 @@ typedef struct rast_tuning {
 
 /* Times the batch under each candidate setting and keeps the fastest in the context (used by
  * rast_render_batch, rast_batch_create and servers created afterwards, where rast_scene.tile is
- * 0): first the bin edge 8/16/32 of both MSAA classes together, then per class the raster
+ * 0): first the bin edge 8/16/32 of both MSAA classes together, under every bin CTA-wide and
+ * under every bin one warp per tile; then, from the best of those, per class the raster
  * kernel split (every bin CTA-wide, bins of 128+, 512+ or 2048+ entries CTA-wide and the rest
  * one warp per tile, every bin one warp per tile) with all the raster CTAs that fit, 4 or 2 per
- * SM; finally one run measures each scene's bins
+ * SM; then the bin edge again under the chosen splits; finally one run measures each scene's bins
  * and the batch reserves that plus an eighth. Images are written to scratch, not the scenes'
  * outputs. No counterpart in the reference (its tile size is the constant TILE_SIZE = 64,
  * src/rasterizer/buffers.rs:8). */

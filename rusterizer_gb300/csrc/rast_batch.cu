@@ -207,26 +207,40 @@ rast_status rast_autotune_batch_ex(rast_ctx* c, const rast_scene* sc, uint32_t n
             if (rep > 0) ms += t / 2.0f;  // the first run sizes buffers
         }
     };
-    // 1. bin edge per MSAA class (8, 16 or 32 pixels), both classes together
+    // 1. bin edge per MSAA class (8, 16 or 32 pixels), both classes together, under each of the
+    // two extreme raster splits (every bin CTA-wide, every bin one warp per tile): the best bin
+    // edge depends on the raster kernel
     const int sizes[3] = {8, 16, 32};
     float best_ms = 3.0e38f;
     int best_tile[2] = {0, 0};
-    for (int a = 0; a < (has[0] ? 3 : 1) && result == RAST_OK; ++a)
-        for (int b = 0; b < (has[1] ? 3 : 1) && result == RAST_OK; ++b) {
-            c->tuned_tile[0] = has[0] ? sizes[a] : 0;
-            c->tuned_tile[1] = has[1] ? sizes[b] : 0;
-            float ms = 0.0f;
-            time_batch(ms);
-            if (result == RAST_OK && ms < best_ms) {
-                best_ms = ms;
-                best_tile[0] = c->tuned_tile[0];
-                best_tile[1] = c->tuned_tile[1];
+    uint32_t best_split = 0;
+    auto sweep_tiles = [&](bool keep_split) {
+        for (int a = 0; a < (has[0] ? 3 : 1) && result == RAST_OK; ++a)
+            for (int b = 0; b < (has[1] ? 3 : 1) && result == RAST_OK; ++b) {
+                c->tuned_tile[0] = has[0] ? sizes[a] : 0;
+                c->tuned_tile[1] = has[1] ? sizes[b] : 0;
+                if (keep_split && c->tuned_tile[0] == best_tile[0] && c->tuned_tile[1] == best_tile[1])
+                    continue;  // the current setting was timed already
+                float ms = 0.0f;
+                time_batch(ms);
+                if (result == RAST_OK && ms < best_ms) {
+                    best_ms = ms;
+                    best_tile[0] = c->tuned_tile[0];
+                    best_tile[1] = c->tuned_tile[1];
+                    if (!keep_split) best_split = E.heavy_bits[0];
+                }
             }
-        }
+    };
+    for (uint32_t split : {0u, 32u}) {
+        E.heavy_bits[0] = E.heavy_bits[1] = split;
+        E.ctas_per_sm[0] = E.ctas_per_sm[1] = 0;
+        sweep_tiles(false);
+    }
+    E.heavy_bits[0] = E.heavy_bits[1] = best_split;
     c->tuned_tile[0] = best_tile[0];
     c->tuned_tile[1] = best_tile[1];
-    // 2. per class: the split between the CTA-wide and the warp-per-tile raster kernel, and
-    // the persistent raster CTAs per SM
+    // 2. per class, from the best of step 1: the split between the CTA-wide and the
+    // warp-per-tile raster kernel, and the persistent raster CTAs per SM
     // every bin CTA-wide; bins of 128+, 512+ or 2048+ entries CTA-wide; every bin one warp each
     const uint32_t heavy_opts[5] = {0u, 7u, 9u, 11u, 32u};
     const int cta_opts[3] = {0, 4, 2};
@@ -250,6 +264,12 @@ rast_status rast_autotune_batch_ex(rast_ctx* c, const rast_scene* sc, uint32_t n
             }
         E.heavy_bits[cls] = bh;
         E.ctas_per_sm[cls] = bc;
+    }
+    // the bin edge again, under the chosen splits
+    if (result == RAST_OK) {
+        sweep_tiles(true);
+        c->tuned_tile[0] = best_tile[0];
+        c->tuned_tile[1] = best_tile[1];
     }
     // 3. bin capacity: one run with the chosen settings measures each scene's bins; the batch
     // reserves that plus an eighth (batch_hints), instead of the first estimate
