@@ -889,8 +889,9 @@ def main():
     ap.add_argument("--nscenes", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+",
                     default=[250, 500, 1000, 2000, 3000, 4000, 6000, 8000, 12000, 14000, 16000, 18000, 20000, 24000, 32000])
-    ap.add_argument("--seconds", type=float, default=1.0)
-    ap.add_argument("--streams", type=int, default=3, help="serving: launch slots of each server")
+    ap.add_argument("--seconds", type=float, default=2.0, help="serving: seconds of arrivals per rate")
+    ap.add_argument("--streams", type=int, default=2, choices=[1, 2],
+                    help="serving: batches in flight at once (the plain server runs one)")
     ap.add_argument("--p99-bound-ms", type=float, default=50.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tile", type=int, default=0)

@@ -219,7 +219,8 @@ typedef struct rast_server rast_server;
 typedef struct rast_server_config {
     uint64_t hbm_budget_bytes; /* in-flight scratch + image bytes admitted at once (0 = 40 GB) */
     uint32_t max_batch;        /* scenes per launch (0 = no limit) */
-    int streams;               /* batches in flight at once, 1 or 2 */
+    int streams;               /* batches in flight at once, 1 or 2 (0 = 2; other values are
+                                  RAST_INVALID_ARG); the plain server always runs one */
     int one_per_launch;        /* 1: plain server, one request per launch */
 } rast_server_config;
 

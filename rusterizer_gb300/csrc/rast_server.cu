@@ -282,7 +282,12 @@ rast_status rast_server_create(rast_ctx* c, const rast_server_config* cfg, rast_
     s->ctx = c;
     c->sync_copies();
     if (cfg) s->cfg = *cfg;
+    if (s->cfg.streams < 0 || s->cfg.streams > 2) {  // 0 takes the default
+        delete s;
+        return RAST_INVALID_ARG;
+    }
     if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = 40ull << 30;
+    if (!s->cfg.streams) s->cfg.streams = 2;
     s->nslots = (s->cfg.streams == 2 && !s->cfg.one_per_launch) ? 2 : 1;
     for (int i = 0; i < s->nslots; ++i) {
         s->slots[i].server = s;

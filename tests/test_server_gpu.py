@@ -168,3 +168,17 @@ def test_request_table_stays_bounded():
     assert (o.cpu().numpy().view(np.uint32).reshape(32, 32) == ref).all()
     srv.close()
     br.close()
+
+
+def test_invalid_stream_count_is_refused():
+    """More than two batches in flight is not offered: the server refuses the configuration
+    instead of quietly running one."""
+    br = BatchRenderer()
+    s = scenes.small_soup(7, ntris=200)
+    br.add_scene(s)
+    for bad in (3, -1):
+        with pytest.raises(_lib.RastError) as e:
+            RenderServer(br, streams=bad)
+        assert e.value.status == _lib.INVALID_ARG
+    RenderServer(br, streams=0).close()  # 0: the default (two)
+    br.close()
