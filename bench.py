@@ -6,8 +6,9 @@ textured fragment shader over a 2048x2048 checkerboard, viewed at 45 degrees so 
 are subpixel. One step is one full frame: vertex stage, clipping/setup, order-preserving
 binning, per-tile raster and resolve. Inputs (mesh, texture) are resident in HBM for `value`; `e2e` streams the mesh from
 pinned host memory through rast_mesh_update and reads the image back every step, from two host
-threads with a context each so that copies overlap kernels (`one_thread_value`: one thread;
-`one_thread_pipelined_value`: one thread with asynchronous mesh updates and image readbacks).
+threads with a context each, each pipelined (asynchronous mesh updates and image readbacks),
+so that copies overlap kernels (`one_thread_value`: one thread, synchronous calls;
+`one_thread_pipelined_value`: one pipelined thread; `two_thread_synchronous_value`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config 0|1|2|3|4] [--impl ours|reference]
 
@@ -473,8 +474,10 @@ def run_ours(args):
     achieved = bytes_frame / (stage_mean[4] / 1000.0) / 1e9  # raster = the frame's HBM traffic
 
     # e2e: stream the mesh from pinned host memory, render, read the image back. Two host
-    # threads, each with its own context (one context per host thread, as the ABI asks), run the
-    # synchronous per-frame calls side by side, so one frame's copies overlap the other's kernels.
+    # threads, each with its own context (one context per host thread, as the ABI asks), run
+    # pipelined lanes side by side (asynchronous mesh updates and image readbacks), so copies
+    # overlap kernels; beside it one thread alone (synchronous, and pipelined) and two threads
+    # with synchronous calls.
     d0 = scene["draws"][0]
     fp = ctypes.POINTER(ctypes.c_float)
     u32p = ctypes.POINTER(ctypes.c_uint32)
@@ -559,29 +562,37 @@ def run_ours(args):
     lanes[0].run(args.steps)
     barrier()
     serial_s = time.perf_counter() - t0
-    # ... and the two lanes together: the e2e number (the same K frames in total)
+    # ... the two synchronous lanes together, and two pipelined lanes together: the e2e number
+    # (the same K frames in total each time)
     import threading
     split = [(args.steps + 1) // 2, args.steps // 2]
-    ths = [threading.Thread(target=ln.run, args=(k,)) for ln, k in zip(lanes, split)]
-    barrier()
-    t0 = time.perf_counter()
-    for th in ths:
-        th.start()
-    for th in ths:
-        th.join()
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_s, serial_s, piped_s = reps.max([e2e_s, serial_s, piped_s])
+    piped2 = PipelinedLane()
+    piped2.run(max(args.warmup, 3))
+
+    def together(pair):
+        ths = [threading.Thread(target=ln.run, args=(k,)) for ln, k in zip(pair, split)]
+        barrier()
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        barrier()
+        return time.perf_counter() - t0
+    sync2_s = together(lanes)
+    e2e_s = together([piped, piped2])
+    e2e_s, serial_s, piped_s, sync2_s = reps.max([e2e_s, serial_s, piped_s, sync2_s])
     e2e_value = world * args.steps / e2e_s
     e2e_serial = world * args.steps / serial_s
     e2e_piped = world * args.steps / piped_s
+    e2e_sync2 = world * args.steps / sync2_s
     queue()
     ref_img = r.framebuffer()
-    for ln in lanes + [piped]:
+    for ln in lanes + [piped, piped2]:
         for o in getattr(ln, "outs", [ln.out]):
             assert (o.numpy().view(np.uint32).reshape(H, W) == ref_img).all(), "e2e image differs"
     h2d = lanes[0].npos.numel() * 4 + lanes[0].nuv.numel() * 4 + lanes[0].nidx.numel() * 4
-    for ln in lanes + [piped]:
+    for ln in lanes + [piped, piped2]:
         ln.r.close()
 
     line = None
@@ -612,7 +623,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": W * H * 4, "host_threads": 2,
-                    "one_thread_value": e2e_serial, "one_thread_pipelined_value": e2e_piped},
+                    "one_thread_value": e2e_serial, "one_thread_pipelined_value": e2e_piped,
+                    "two_thread_synchronous_value": e2e_sync2},
             "gpu_launches": timed_launches,
             "clocks": clk.summary(),
         }
