@@ -172,6 +172,16 @@ class Renderer:
         check(_lib.load().rast_mesh_update(self._ctx, h, pos.ctypes.data_as(_fp), uv.ctypes.data_as(_fp),
                                            rg, idx.ctypes.data_as(_u32p)), "mesh update")
 
+    def update_async(self, mesh, pos, uv, idx, rgba=None):
+        """Like update(), with the copies on a side stream after the frames already enqueued; the
+        next frame that draws this mesh waits for them on the device. The arrays must stay
+        unchanged until that frame is done (page-locked arrays make the copies asynchronous)."""
+        h = self.upload(mesh)
+        ptr = lambda a: ctypes.cast(_data_ptr(a), _fp)  # noqa: E731
+        check(_lib.load().rast_mesh_update_async(self._ctx, h, ptr(pos), ptr(uv),
+                                                 None if rgba is None else ptr(rgba),
+                                                 ctypes.cast(_data_ptr(idx), _u32p)), "mesh update")
+
     def render(self, mesh, vertex_shader=VS_MVP, fragment_shader=FS_TEXTURE):
         """Renderer::render (src/render.rs:98-114): queue the mesh with the current uniforms."""
         L = _lib.load()
@@ -193,6 +203,21 @@ class Renderer:
         if st not in (_lib.OK, _lib.TEXTURE_OOB):
             raise RastError(st, "framebuffer")
         return out
+
+    def framebuffer_async(self, out):
+        """Enqueue the frame without waiting (rast_framebuffer_async). `out` is a device pointer,
+        a CUDA tensor, or host memory (a numpy array or a page-locked CPU tensor): the image is
+        then copied out on a side stream while the next frame renders, and is complete after
+        wait_output(out). No overflow re-run: capacities come from earlier framebuffer() calls."""
+        st = _lib.load().rast_framebuffer_async(self._ctx, ctypes.c_void_p(_data_ptr(out)))
+        if st not in (_lib.OK, _lib.TEXTURE_OOB):
+            raise RastError(st, "framebuffer_async")
+        return st
+
+    def wait_output(self, out=None):
+        """Wait for the asynchronous copies into host array `out` (all of them when None)."""
+        check(_lib.load().rast_wait_output(self._ctx, None if out is None else ctypes.c_void_p(_data_ptr(out))),
+              "wait_output")
 
     def display(self):
         """Headless stand-in for Renderer::display (src/render.rs:116-127)."""
@@ -235,6 +260,15 @@ class Renderer:
         ms = (ctypes.c_float * 5)()
         n = _lib.load().rast_stage_times(self._ctx, ms, 5)
         return list(ms[:n])
+
+
+def _data_ptr(a):
+    """Address of a numpy array, a torch tensor or a plain integer pointer."""
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())
 
 
 def render_scene(scene, tile=0, capture=False, log_capacity=0, renderer=None, heavy_entries=None):

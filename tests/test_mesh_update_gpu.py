@@ -57,7 +57,11 @@ def test_async_updates_of_two_meshes_in_turn():
     for k in range(len(order)):
         # the next frame's data goes to the other mesh while this frame renders
         if k + 1 < len(order):
-            send(L.rast_mesh_update_async, k + 1)
+            if k % 2:  # through the Python mirror
+                p, u, i = data[order[k + 1]]
+                r.update_async(slots[(k + 1) % 2], p, u, i)
+            else:
+                send(L.rast_mesh_update_async, k + 1)
         r.render(slots[k % 2], renderer.VS_MVP, 0)
         st = L.rast_framebuffer(r._ctx, ctypes.c_void_p(out.data_ptr()))
         assert st == _lib.OK, st
@@ -98,13 +102,19 @@ def test_async_frames_into_host_memory():
     for outs, ptr in ((pinned, lambda o: o.data_ptr()), (pageable, lambda o: o.ctypes.data)):
         for k in range(len(worlds)):
             frame(k)
-            assert L.rast_framebuffer_async(r._ctx, ctypes.c_void_p(ptr(outs[k % 2]))) == _lib.OK
+            if outs is pinned:  # through the C ABI
+                assert L.rast_framebuffer_async(r._ctx, ctypes.c_void_p(ptr(outs[k % 2]))) == _lib.OK
+            else:  # through the Python mirror
+                r.framebuffer_async(outs[k % 2])
             if k:
                 prev = outs[(k - 1) % 2]
-                assert L.rast_wait_output(r._ctx, ctypes.c_void_p(ptr(prev))) == _lib.OK
+                if outs is pinned:
+                    assert L.rast_wait_output(r._ctx, ctypes.c_void_p(ptr(prev))) == _lib.OK
+                else:
+                    r.wait_output(prev)
                 got = prev.numpy() if hasattr(prev, "numpy") else prev
                 assert (got.view(np.uint32).reshape(H, W) == want[k - 1]).all(), k - 1
-        assert L.rast_wait_output(r._ctx, None) == _lib.OK
+        r.wait_output()
         last = outs[(len(worlds) - 1) % 2]
         got = last.numpy() if hasattr(last, "numpy") else last
         assert (got.view(np.uint32).reshape(H, W) == want[-1]).all()
