@@ -588,6 +588,10 @@ typedef struct {
     oracle_ctx* c;
     const rec* const* part_recs; /* the block's records, in submission order, in nparts parts */
     const size_t* part_n;
+    /* with several bands: per part, the indices of its records whose rows meet each band
+     * (band b's at band_idx[part][band_off[part][b] .. band_off[part][b + 1])), in order */
+    uint32_t* const* band_idx;
+    size_t* const* band_off;
     int nparts;
     int fs_id;
     uint64_t band, nbands;
@@ -634,16 +638,22 @@ static void shade_and_write(oracle_ctx* c, const rec* r, int fs_id, uint64_t x, 
     (*fsinv)++;
 }
 
-/* Per-triangle pixel loop of Rasterizer::rasterize, mod.rs:443-473, over the rows of band
- * `band` of `nbands`: the rows whose 64-row tile row is band modulo nbands (every row when
- * nbands is 1). Bands share no tile, so they run on separate threads. */
+/* Per-triangle pixel loop of Rasterizer::rasterize, mod.rs:443-473, over the pixels of band
+ * `band` of `nbands`: the 64x64 tiles (tile row tr, tile column tc) with (tr + tc) modulo
+ * nbands equal to band (every pixel when nbands is 1). The diagonal interleave spreads a strip
+ * of the screen, rows or columns, over every band. Bands share no tile, so they run on separate
+ * threads; each visits the pixels of a box in the reference's row-major order. */
 static void raster_rec(oracle_ctx* c, const rec* r, int fs_id, uint64_t band, uint64_t nbands,
                        uint64_t* shaded, uint64_t* fsinv, uint64_t* oobc) {
     const int S = c->msaa;
     const float(*pat)[2] = S == 4 ? RGSS4 : CENTRE1;
     for (uint64_t y = r->by0; y < r->by1; ++y) {
-        if (nbands > 1 && (y / TILE_SIZE) % nbands != band) continue;
+        const uint64_t tr = y / TILE_SIZE;
         for (uint64_t x = r->bx0; x < r->bx1; ++x) {
+            if (nbands > 1 && (tr + x / TILE_SIZE) % nbands != band) {
+                x = (x / TILE_SIZE + 1) * TILE_SIZE - 1;  /* to the next tile column */
+                continue;
+            }
             float e[4][3];
             unsigned cov = 0;
             for (int i = 0; i < S; ++i) {
@@ -676,9 +686,16 @@ static void* band_main(void* arg) {
     band_job* j = (band_job*)arg;
     /* counted in locals: the jobs of neighbouring bands share cache lines */
     uint64_t shaded = 0, fsinv = 0, oob = 0;
-    for (int p = 0; p < j->nparts; ++p)
-        for (size_t i = 0; i < j->part_n[p]; ++i)
-            raster_rec(j->c, &j->part_recs[p][i], j->fs_id, j->band, j->nbands, &shaded, &fsinv, &oob);
+    for (int p = 0; p < j->nparts; ++p) {
+        if (j->nbands > 1) {
+            const uint32_t* L = j->band_idx[p];
+            for (size_t i = j->band_off[p][j->band]; i < j->band_off[p][j->band + 1]; ++i)
+                raster_rec(j->c, &j->part_recs[p][L[i]], j->fs_id, j->band, j->nbands, &shaded, &fsinv, &oob);
+        } else {
+            for (size_t i = 0; i < j->part_n[p]; ++i)
+                raster_rec(j->c, &j->part_recs[p][i], j->fs_id, j->band, j->nbands, &shaded, &fsinv, &oob);
+        }
+    }
     j->shaded = shaded;
     j->fsinv = fsinv;
     j->oob = oob;
@@ -746,7 +763,35 @@ typedef struct {
     rec** part_recs;
     size_t* part_n;
     uint32_t* part_status;
+    int nbands;            /* > 1: also list each part's records by band (band_main) */
+    uint32_t** band_idx;   /* per part, grown as needed (band_cap entries) */
+    size_t* band_cap;
+    size_t** band_off;     /* per part, nbands + 1 offsets */
 } setup_job;
+
+/* The bands ((tile row + tile column) modulo nbands) whose tiles a record's box meets: the
+ * diagonals from (tr0 + tc0) to (tr1 + tc1); calls add(b) once per band. Records with an empty
+ * box meet none. */
+static void rec_bands(const rec* r, int nbands, void (*add)(void*, int), void* arg) {
+    if (r->by0 >= r->by1 || r->bx0 >= r->bx1) return;
+    const uint64_t d0 = r->by0 / TILE_SIZE + r->bx0 / TILE_SIZE;
+    const uint64_t d1 = (r->by1 - 1) / TILE_SIZE + (r->bx1 - 1) / TILE_SIZE;
+    if (d1 - d0 + 1 >= (uint64_t)nbands) {
+        for (int b = 0; b < nbands; ++b) add(arg, b);
+        return;
+    }
+    for (uint64_t d = d0; d <= d1; ++d) add(arg, (int)(d % (uint64_t)nbands));
+}
+typedef struct {
+    size_t* off;
+    uint32_t* idx;
+    uint32_t rec;
+} band_fill;
+static void band_count_add(void* a, int b) { ((band_fill*)a)->off[b + 1]++; }
+static void band_fill_add(void* a, int b) {
+    band_fill* f = (band_fill*)a;
+    f->idx[f->off[b]++] = f->rec;
+}
 static void setup_part(void* a, int part, int nparts) {
     setup_job* j = (setup_job*)a;
     size_t n = j->t1 - j->t0;
@@ -771,6 +816,28 @@ static void setup_part(void* a, int part, int nparts) {
     j->part_recs[part] = out;
     j->part_n[part] = k;
     j->part_status[part] = status;
+    if (j->nbands > 1) {
+        /* counting sort of the part's record indices by band, keeping their order */
+        const int nb = j->nbands;
+        size_t* off = j->band_off[part];
+        for (int b = 0; b <= nb; ++b) off[b] = 0;
+        band_fill f = {off, NULL, 0};
+        for (size_t i = 0; i < k; ++i) rec_bands(&out[i], nb, band_count_add, &f);
+        for (int b = 0; b < nb; ++b) off[b + 1] += off[b];
+        if (off[nb] > j->band_cap[part]) {
+            free(j->band_idx[part]);
+            j->band_cap[part] = off[nb] + off[nb] / 2;
+            j->band_idx[part] = (uint32_t*)malloc(sizeof(uint32_t) * j->band_cap[part]);
+        }
+        f.idx = j->band_idx[part];
+        for (size_t i = 0; i < k; ++i) {
+            f.rec = (uint32_t)i;
+            rec_bands(&out[i], nb, band_fill_add, &f);
+        }
+        /* the fill advanced each band's start to its end: shift back */
+        for (int b = nb; b > 0; --b) off[b] = off[b - 1];
+        off[0] = 0;
+    }
 }
 
 /* One draw's pixel work on a pool of threads created once per draw: per block of triangles,
@@ -822,8 +889,8 @@ static void* draw_worker_main(void* arg) {
         }
         spin_barrier_wait(&P->bar, &sense);
         if (w->k < P->nbands) {
-            band_job b = {P->c, (const rec* const*)P->sj->part_recs, P->sj->part_n, nparts, P->fs_id,
-                          (uint64_t)w->k, (uint64_t)P->nbands, 0, 0, 0};
+            band_job b = {P->c, (const rec* const*)P->sj->part_recs, P->sj->part_n, P->sj->band_idx,
+                          P->sj->band_off, nparts, P->fs_id, (uint64_t)w->k, (uint64_t)P->nbands, 0, 0, 0};
             band_main(&b);
             w->shaded += b.shaded;
             w->fsinv += b.fsinv;
@@ -865,7 +932,7 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
     rec** part_recs = (rec**)calloc((size_t)nthreads, sizeof(rec*));
     size_t* part_n = (size_t*)calloc((size_t)nthreads, sizeof(size_t));
     uint32_t* part_status = (uint32_t*)calloc((size_t)nthreads, sizeof(uint32_t));
-    setup_job sj = {c, clip, uv, rgba, idx, 0, 0, recs, maxper, part_recs, part_n, part_status};
+    setup_job sj = {c, clip, uv, rgba, idx, 0, 0, recs, maxper, part_recs, part_n, part_status, 1, NULL, NULL, NULL};
     uint64_t shaded = 0, fsinv = 0, oob = 0;
     if (nthreads == 1) {
         for (size_t t0 = 0; t0 < ntris; t0 += BLOCK) {
@@ -877,9 +944,11 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
                 raster_rec(c, &part_recs[0][i], fs_id, 0, 1, &shaded, &fsinv, &oob);
         }
     } else {
-        /* bands of interleaved 64-row tile rows (row r to band r % nb): no two threads mark one
-         * tile, and uneven scenes spread over every band */
-        const uint64_t rows_tiles = ((uint64_t)c->h + TILE_SIZE - 1) / TILE_SIZE;
+        /* bands of 64x64 tiles interleaved along the diagonals ((tile row + tile column) % nb):
+         * no two threads mark one tile, and a block of triangles that covers a strip of the
+         * screen still spreads over every band */
+        const uint64_t rows_tiles = ((uint64_t)c->h + TILE_SIZE - 1) / TILE_SIZE +
+                                    ((uint64_t)c->w + TILE_SIZE - 1) / TILE_SIZE - 1;
         draw_pool P;
         P.c = c;
         P.sj = &sj;
@@ -887,6 +956,11 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
         P.block = BLOCK;
         P.nthreads = nthreads;
         P.nbands = (uint64_t)nthreads > rows_tiles ? (int)rows_tiles : nthreads;
+        sj.nbands = P.nbands;
+        sj.band_idx = (uint32_t**)calloc((size_t)nthreads, sizeof(uint32_t*));
+        sj.band_cap = (size_t*)calloc((size_t)nthreads, sizeof(size_t));
+        sj.band_off = (size_t**)calloc((size_t)nthreads, sizeof(size_t*));
+        for (int k = 0; k < nthreads; ++k) sj.band_off[k] = (size_t*)calloc((size_t)P.nbands + 1, sizeof(size_t));
         P.fs_id = fs_id;
         atomic_init(&P.bar.count, 0);
         atomic_init(&P.bar.sense, 0);
@@ -907,6 +981,13 @@ uint32_t oracle_draw(oracle_ctx* c, const float* pos, const float* uv, const flo
         }
         free(ws);
         free(th);
+        for (int k = 0; k < nthreads; ++k) {
+            free(sj.band_idx[k]);
+            free(sj.band_off[k]);
+        }
+        free(sj.band_idx);
+        free(sj.band_cap);
+        free(sj.band_off);
     }
     free(part_recs);
     free(part_n);
