@@ -381,8 +381,9 @@ def run_reference(args):
         "shaded_samples_per_s": shaded * fps,
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} full frames (draw + framebuffer on one renderer), "
-                                   f"{cores} threads: triangle setup in parts, pixels in bands of "
-                                   "interleaved 64-row tile rows (the reference crate is Rust; no toolchain here)"},
+                                   f"{cores} threads: triangle setup in parts, pixels in 64x64 tiles "
+                                   "interleaved along diagonals between the threads (the reference crate is "
+                                   "Rust; no toolchain here)"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
