@@ -52,6 +52,18 @@ def launches_per_frame(width, height, ntris, tile=0):
     return 8 if tile == 32 else 7
 
 
+def sustained_point(sweep, bound_ms):
+    """The sweep point of the highest offered rate whose p99 and every lower rate's p99 are
+    within the bound (a rate past saturation can pass a short window by luck after a lower one
+    failed); None when the lowest rate already fails. `sweep` is in increasing offered rate."""
+    best = None
+    for st in sweep:
+        if st["p99_ms"] > bound_ms:
+            break
+        best = st
+    return best
+
+
 def batch_tile(scene, tuned):
     """Bin size of a scene in the batch: the autotuned one of its MSAA class, else the library's
     automatic choice (launches_per_frame)."""
@@ -834,14 +846,7 @@ def run_serving(args):
             sampler.__exit__(None, None, None)
             clk = sampler.summary()
         srv.close()
-        # the sustained rate: the highest offered rate of the sweep's passing prefix (a rate past
-        # saturation can pass a one-second window by luck after a lower one failed)
-        ok = []
-        for st_ in sweep:
-            if st_["p99_ms"] > bound:
-                break
-            ok.append(st_)
-        best = ok[-1] if ok else None
+        best = sustained_point(sweep, bound)
         results[mode] = {"sweep": sweep, "max_rate_within_bound": best["offered_rate"] if best else 0.0,
                          "at_max": best}
     br.close()

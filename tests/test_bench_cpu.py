@@ -41,3 +41,12 @@ def test_committed_profile(bench):
     assert bench.committed_profile(1) > 0 and bench.committed_profile(2) > 0
     assert 0.0 < bench.committed_profile(1, "issue_active") <= 1.0
     assert bench.committed_profile(0) is None and bench.committed_profile(0, "issue_active") is None
+
+
+def test_sustained_rate_is_the_passing_prefix(bench):
+    sweep = [{"offered_rate": r, "p99_ms": p} for r, p in
+             [(1000, 1.0), (2000, 2.0), (4000, 40.0), (6000, 137.0), (8000, 8.0)]]
+    assert bench.sustained_point(sweep, 50.0)["offered_rate"] == 4000  # 8000 passed by luck
+    assert bench.sustained_point(sweep, 1.5)["offered_rate"] == 1000
+    assert bench.sustained_point(sweep, 0.5) is None
+    assert bench.sustained_point([], 50.0) is None
