@@ -1,14 +1,20 @@
 // rast_kernels.cu - sm_103a kernels of the raster pipeline.
 //
 //   k_vertex       per vertex: MVP * v, divide, viewport, clip predicates       (HBM-bound)
-//   k_bin_count    per chunk of triangles: classify/clip, tile rectangle, per-chunk tile
-//                  histogram in shared memory
+//   k_bin_count    per chunk of triangles: classify, tile rectangle, per-chunk tile histogram
+//                  in shared memory (band by band for frames of more than 16384 bins)
+//   k_clip         one warp per triangle that straddles a clip plane: clip, fan boxes, counts
 //   k_scan_cols    per tile: exclusive prefix of the histograms over chunks
-//   k_scan_tiles   per frame: exclusive prefix over tiles -> bin ranges, capacity check
+//   k_scan_tiles   per frame: exclusive prefix over tiles -> bin ranges, capacity check; for a
+//                  one-frame run also the raster tile queue
 //   k_bin_scatter  per chunk: order-preserving scatter of triangle ids into tile bins
-//   k_raster<S,TS> per tile: replays the tile's triangles in submission order with all
-//                  colour/depth samples in shared memory; coverage, depth test,
-//                  perspective-correct interpolation, fragment shader, resolve, store
+//   k_tile_order   per raster launch of a batch: the raster tile queue, heaviest first
+//   k_bin_split    per 32-pixel bin: its entries split into four 16-pixel quadrant lists
+//   k_raster<S,TS> per raster tile, a CTA of 4 warps: replays the tile's triangles in
+//                  submission order with all colour/depth samples in shared memory; coverage,
+//                  depth test, perspective-correct interpolation, fragment shader, resolve
+//   k_raster_warp  the same with one warp per raster tile, for light tiles
+//                  (rast_raster_warp.cuh)
 //
 // No kernel waits on another CTA; every loop is bounded by sizes read from descriptors.
 #include <cuda_runtime.h>

@@ -4,14 +4,14 @@
 // partial warps between block barriers. Here one warp owns a whole tile: it stages the tile's
 // items 32 at a time, one per lane and held in that lane's registers (other lanes read them
 // with shuffles, which keeps shared memory for the samples and rings: 5 CTAs of 4 warps per
-// SM), walks their candidate pixels 32 at a time, depth-tests the covered fragments in
+// SM with four samples per pixel, 6 with one), walks their candidate pixels 32 at a time, depth-tests the covered fragments in
 // submission order and shades the passed ones, with full warps and no block barrier. The
 // arithmetic is the same device functions as k_raster (coverage, sample depths, tie rule,
 // interpolation, shaders, resolve), so results are bit-identical; only the work split differs.
 //
 // The persistent kernel takes light tiles (bins past the first `nheavy` of the raster queue,
-// which k_tile_order sorts heaviest first) from their own counter, then helps clear the bins
-// without entries. k_raster takes the heavy tiles.
+// which k_tile_order or, for a one-frame run, k_scan_tiles sorts heaviest first) from their own
+// counter, then helps clear the bins without entries. k_raster takes the heavy tiles.
 
 constexpr int kWarpUnitWarps = 4;  // warps (independent tiles) per CTA of k_raster_warp
 // CTAs per SM the launch bounds aim at: with 4 samples the shared sample tiles allow 5; with
