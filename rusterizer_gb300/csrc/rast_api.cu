@@ -3,9 +3,11 @@
 // A context owns: resident meshes and textures, a CUDA stream, the scratch buffers of the
 // pipeline (grown on demand and kept across frames), a pinned staging area for the per-frame
 // descriptors, and a small device state block (status bits, statistics, allocation counters).
-// A frame is one descriptor upload, one state reset, six kernel launches and one state
-// readback; capacity overflows (bins, clip store) are detected on the device and the frame is
-// re-run once with the measured sizes.
+// A frame is one descriptor upload (skipped when the descriptors are unchanged), one state
+// reset, seven kernel launches (eight with 32-pixel bins) and one state readback; capacity
+// overflows (bins, clip store) are detected on the device and the frame is re-run with the
+// measured sizes (at most twice). rast_framebuffer_async skips the readback; into host memory it
+// resolves into alternating staging buffers that a side stream copies out.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -5,7 +5,10 @@
 // kernels run once over every scene, and the persistent raster kernel (one launch per
 // (MSAA, tile size) class) takes tiles of all scenes from a single queue, heaviest first, so
 // uneven scenes share the GPU instead of each occupying it for a launch of its own. Scenes are
-// independent, so each scene's image is bit-identical to rendering it alone.
+// independent, so each scene's image is bit-identical to rendering it alone. Scenes with host
+// outputs resolve into a staging buffer that is copied out at the end (in a captured batch,
+// inside the graph, so two batches launched in turn overlap one's copies with the other's
+// kernels).
 #include <cuda_runtime.h>
 
 #include <algorithm>
